@@ -1,0 +1,253 @@
+// Device-side tables, shared-memory layout and small helpers of the GB300 chunk mesher.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hc_flow.h"
+#include "hc_registry.h"
+
+namespace hc {
+
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+constexpr int kChunk = 32;
+constexpr int kQuadsPerMesh = 16383;       // 65,532 vertices: the uint16 split point (BlockMeshAlgo.hpp:274)
+constexpr int kMaxMeshesPerStream = 48;    // > 720,896 / 16,383
+constexpr int kPlanes = 198;               // 3 axes x 33 slices x 2 face directions
+constexpr int kSlices = 99;
+constexpr int kSegments = kPlanes + 1;     // segment 0 = custom meshes, then the planes in output order
+
+// Staged block classes cover x, z in [-2, 33] and y in [-1, 32]: the mesher reads [-1, 32]^3 and
+// a flowing liquid on that ring looks one more cell out horizontally (Liquid.hpp:406-415).
+constexpr int kClsX = 36, kClsY = 34, kClsZ = 36;
+constexpr int kClsCells = kClsX * kClsY * kClsZ; // 44,064
+// Light of [-1, 32]^3, the region the mesher reads.
+constexpr int kLt = 34;
+constexpr int kLtCells = kLt * kLt * kLt; // 39,304
+// The relight window [-15, 47)^3 as 62 x 62 rows of 62-bit words (bit = x + 15).
+constexpr int kWin = 62;
+constexpr int kWinRows = kWin * kWin; // 3,844
+
+// One block class: a distinct property row of the registry (65,536 raw values map onto < 256).
+struct DevClass {
+	uint16_t tex[6];
+	uint8_t flags;     // kF* below
+	uint8_t light;     // light level
+	uint8_t mesh_first;// first static face (static meshes)
+	uint8_t mesh_meta; // kind | count_or_variant << 2
+};
+static_assert(sizeof(DevClass) == 16, "DevClass is 16 bytes");
+
+enum : uint8_t {
+	kFIndirect = 1,   // transparency != opaque (light passes, BFS may enter)
+	kFDirect = 2,     // vertical pass or no solid collision (AO does not darken)
+	kFVertical = 4,   // transparency == transparent
+	kFOpaqueCube = 8, // six non-empty, non-transparent textures and no custom mesh
+	kFEmpty = 16,     // six empty textures and no custom mesh
+	kFTagShift = 5    // 2-bit id tag
+};
+enum : uint8_t { kTagOther = 0, kTagAir = 1, kTagSource = 2, kTagFlow = 3 };
+
+struct DevTables {
+	const uint8_t *class_of;  // [65536]
+	const DevClass *classes;  // [256]
+};
+
+// Texture flags (one bit per texture id) and static custom-mesh faces.
+__constant__ uint64_t c_tex_transparent;
+__constant__ uint64_t c_tex_liquid;
+__constant__ uint64_t c_tex_transpass;
+__constant__ hc_mesh_face c_static_faces[HC_MAX_STATIC_FACES / 4];
+
+// Per-face neighbour offsets: the face-front cell, and per corner {side 0, diagonal, side 1}
+// (client/include/client/BlockMeshAlgo.hpp:74-108).
+__constant__ int8_t c_front[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+__constant__ int8_t c_corner[6][4][3][3] = {
+    {{{1, 0, -1}, {1, -1, -1}, {1, -1, 0}},
+     {{1, 0, -1}, {1, 1, -1}, {1, 1, 0}},
+     {{1, 0, 1}, {1, 1, 1}, {1, 1, 0}},
+     {{1, 0, 1}, {1, -1, 1}, {1, -1, 0}}},
+    {{{-1, 0, -1}, {-1, -1, -1}, {-1, -1, 0}},
+     {{-1, 0, 1}, {-1, -1, 1}, {-1, -1, 0}},
+     {{-1, 0, 1}, {-1, 1, 1}, {-1, 1, 0}},
+     {{-1, 0, -1}, {-1, 1, -1}, {-1, 1, 0}}},
+    {{{0, 1, -1}, {-1, 1, -1}, {-1, 1, 0}},
+     {{0, 1, 1}, {-1, 1, 1}, {-1, 1, 0}},
+     {{0, 1, 1}, {1, 1, 1}, {1, 1, 0}},
+     {{0, 1, -1}, {1, 1, -1}, {1, 1, 0}}},
+    {{{0, -1, -1}, {-1, -1, -1}, {-1, -1, 0}},
+     {{0, -1, -1}, {1, -1, -1}, {1, -1, 0}},
+     {{0, -1, 1}, {1, -1, 1}, {1, -1, 0}},
+     {{0, -1, 1}, {-1, -1, 1}, {-1, -1, 0}}},
+    {{{0, -1, 1}, {-1, -1, 1}, {-1, 0, 1}},
+     {{0, -1, 1}, {1, -1, 1}, {1, 0, 1}},
+     {{0, 1, 1}, {1, 1, 1}, {1, 0, 1}},
+     {{0, 1, 1}, {-1, 1, 1}, {-1, 0, 1}}},
+    {{{0, -1, -1}, {-1, -1, -1}, {-1, 0, -1}},
+     {{0, 1, -1}, {-1, 1, -1}, {-1, 0, -1}},
+     {{0, 1, -1}, {1, 1, -1}, {1, 0, -1}},
+     {{0, -1, -1}, {1, -1, -1}, {1, 0, -1}}}};
+
+// Shared memory of one chunk CTA (about 192 KB: one CTA per SM).
+struct Relight {
+	uint64_t pass[kWinRows];    // blocks light may enter
+	uint64_t sun[kWinRows];     // current level set of the sun channel
+	uint64_t torch[kWinRows];   // current level set of the torch channel
+	uint32_t low_rows[(kWinRows + 31) / 32]; // rows holding emitters of level 1..14
+};
+struct Smem {
+	DevClass classes[256];
+	const uint16_t *blk[27];
+	const int8_t *hgt[27];
+	alignas(16) uint8_t cls[kClsCells];
+	alignas(16) uint8_t light[kLtCells + 8];
+	union {
+		Relight rl;
+		uint32_t masks[kPlanes][32][4]; // per plane row: visible, equal-right, equal-below, transparent pass
+	} u;
+	uint32_t seg_cnt[2][kSegments + 1];
+	uint32_t seg_base[3][kSegments + 1]; // per stream and all-stream exclusive prefix
+	uint32_t warp_sum[3][kWarps];
+	uint32_t aabb[2][kMaxMeshesPerStream][6];
+	uint32_t trig[2][kMaxMeshesPerStream];
+	uint32_t misc[16];
+};
+
+__device__ __forceinline__ int cls_index(int x, int y, int z) { return ((y + 1) * kClsZ + (z + 2)) * kClsX + (x + 2); }
+__device__ __forceinline__ int lt_index(int x, int y, int z) { return ((y + 1) * kLt + (z + 1)) * kLt + (x + 1); }
+
+// Neighbour chunk index of a cell in [-32, 64)^3 (common/include/common/Position.hpp:138-145).
+__device__ __forceinline__ int nb_index(int x, int y, int z) {
+	int cx = x < 0 ? 1 : (x >= kChunk ? 0 : 2);
+	int cy = y < 0 ? 1 : (y >= kChunk ? 0 : 2);
+	int cz = z < 0 ? 1 : (z >= kChunk ? 0 : 2);
+	return cx * 9 + cy * 3 + cz;
+}
+__device__ __forceinline__ uint16_t raw_at(const Smem &S, int x, int y, int z) {
+	return S.blk[nb_index(x, y, z)][(x & 31) + ((y & 31) * kChunk + (z & 31)) * kChunk];
+}
+// Chunk::GetSunlight: unsigned local y >= the int8 height converted to unsigned (Chunk.hpp:74-76).
+__device__ __forceinline__ bool sunlit(const Smem &S, int x, int y, int z) {
+	int8_t h = S.hgt[nb_index(x, y, z)][(x & 31) + (z & 31) * kChunk];
+	return (uint32_t)(y & 31) >= (uint32_t)(int32_t)h;
+}
+
+__device__ __forceinline__ bool tex_transparent(uint16_t t) { return (c_tex_transparent >> (t & 63u)) & 1u; }
+__device__ __forceinline__ bool tex_liquid(uint16_t t) { return (c_tex_liquid >> (t & 63u)) & 1u; }
+__device__ __forceinline__ bool tex_transpass(uint16_t t) { return (c_tex_transpass >> (t & 63u)) & 1u; }
+__device__ __forceinline__ bool tex_empty(uint16_t t) { return (t & 0x1fffu) == 0; }
+
+// BlockTexture::Show (texture/include/texture/BlockTexture.hpp:68-76).
+__device__ __forceinline__ bool show(uint16_t a, uint16_t b) {
+	if (tex_empty(a) || a == b)
+		return false;
+	const bool ta = tex_transparent(a), tb = tex_transparent(b);
+	if (!ta && !tb)
+		return false;
+	if (tex_liquid(a) && !tex_empty(b))
+		return false;
+	return !ta || tb || tex_liquid(b);
+}
+
+__device__ __forceinline__ uint8_t class_at(const Smem &S, int x, int y, int z) { return S.cls[cls_index(x, y, z)]; }
+__device__ __forceinline__ uint8_t tag_of(const DevClass &k) { return k.flags >> kFTagShift; }
+
+// Dynamic face textures of a flowing liquid at (x, y, z) in [-1, 32]^3.
+__device__ void flow_mesh_at(const Smem &S, int x, int y, int z, uint8_t variant, hc_mesh_face *faces, uint32_t *count,
+                             uint16_t tex6[6]) {
+	const int kF[8][2] = {{-1, -1}, {0, -1}, {1, -1}, {-1, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
+	uint16_t nei[8];
+#pragma unroll
+	for (int i = 0; i < 8; ++i)
+		nei[i] = raw_at(S, x + kF[i][0], y, z + kF[i][1]);
+	hc_flow_mesh_impl(nei, variant, faces, count, tex6);
+}
+
+// Face texture of the block at (x, y, z), honouring flowing-liquid dynamic textures
+// (BlockMeshAlgo.hpp:322-326).
+__device__ __forceinline__ uint16_t get_tex(const Smem &S, int x, int y, int z, int face) {
+	const DevClass &k = S.classes[class_at(S, x, y, z)];
+	if (tag_of(k) == kTagFlow) {
+		uint16_t t6[6];
+		uint32_t n;
+		flow_mesh_at(S, x, y, z, (uint8_t)(k.mesh_meta >> 2), nullptr, &n, t6);
+		return t6[face];
+	}
+	return k.tex[face];
+}
+
+// Swizzle YZX (client/include/client/BlockAlgo.hpp:30-41, 70-81): plane axes (U, V) are (y, z) for
+// x slices, (z, x) for y slices and (y, x) for z slices.
+__device__ __forceinline__ void to_xyz(int axis, int a, int u, int v, int &x, int &y, int &z) {
+	if (axis == 0)
+		x = a, y = u, z = v;
+	else if (axis == 1)
+		x = v, y = a, z = u;
+	else
+		x = v, y = u, z = a;
+}
+
+// Light4 of a face (BlockMeshAlgo.hpp:48-163): per corner a 2-bit AO and smoothed sun / torch
+// light in 0..60. Packed as sun bytes, torch bytes and the AO byte.
+struct Light4 {
+	uint32_t sun, torch, ao;
+};
+
+__device__ __forceinline__ uint32_t div_small(uint32_t v, uint32_t n) { return v / n; }
+
+__device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
+	const int fx = x + c_front[face][0], fy = y + c_front[face][1], fz = z + c_front[face][2];
+	const DevClass &kf = S.classes[class_at(S, fx, fy, fz)];
+	const bool dp3 = kf.flags & kFDirect;
+	const uint8_t lf = S.light[lt_index(fx, fy, fz)];
+	Light4 r{0, 0, 0};
+#pragma unroll
+	for (int v = 0; v < 4; ++v) {
+		bool ip[3], dp[3];
+		uint8_t l[3];
+#pragma unroll
+		for (int b = 0; b < 3; ++b) {
+			const int cx = x + c_corner[face][v][b][0], cy = y + c_corner[face][v][b][1], cz = z + c_corner[face][v][b][2];
+			const uint8_t fl = S.classes[class_at(S, cx, cy, cz)].flags;
+			ip[b] = fl & kFIndirect;
+			dp[b] = fl & kFDirect;
+			l[b] = S.light[lt_index(cx, cy, cz)];
+		}
+		const int blocked = !dp[0] + !dp[1] + !dp[2] + !dp3;
+		const uint32_t ao = ((!dp[0] && !dp[2]) || (!dp[1] && !dp3)) ? 0u : (uint32_t)(3 - blocked > 0 ? 3 - blocked : 0);
+		uint32_t counter = 1, sun = lf & 15u, torch = lf >> 4;
+		if (ip[0] || ip[2]) {
+#pragma unroll
+			for (int b = 0; b < 3; ++b)
+				if (ip[b]) {
+					++counter;
+					sun += l[b] & 15u;
+					torch += l[b] >> 4;
+				}
+		}
+		r.ao |= ao << (2 * v);
+		r.sun |= div_small(sun << 2, counter) << (8 * v);
+		r.torch |= div_small(torch << 2, counter) << (8 * v);
+	}
+	return r;
+}
+
+__device__ __forceinline__ uint32_t l4_get(uint32_t packed, int i) { return (packed >> (8 * i)) & 0xffu; }
+__device__ __forceinline__ uint32_t ao_get(uint32_t ao, int i) { return (ao >> (2 * i)) & 3u; }
+
+// Light4::GetFlip (BlockMeshAlgo.hpp:38-43).
+__device__ __forceinline__ bool flip_of(const Light4 &l) {
+	int a = (int)((ao_get(l.ao, 0) + 1) * (l4_get(l.sun, 0) + 1)) - (int)((ao_get(l.ao, 2) + 1) * (l4_get(l.sun, 2) + 1));
+	int b = (int)((ao_get(l.ao, 1) + 1) * (l4_get(l.sun, 1) + 1)) - (int)((ao_get(l.ao, 3) + 1) * (l4_get(l.sun, 3) + 1));
+	return abs(a) < abs(b);
+}
+
+// Packed vertex (client/include/client/BlockVertex.hpp:13-17).
+__device__ __forceinline__ uint2 pack_vertex(uint32_t x, uint32_t y, uint32_t z, uint32_t axis, uint32_t face, uint32_t ao,
+                                             uint32_t sun, uint32_t torch, uint16_t texture) {
+	uint32_t id = texture & 0x1fffu, trans = (uint32_t)texture >> 13;
+	return make_uint2(x | (y << 10u) | (z << 20u) | (axis << 30u),
+	                  (id - 1u) | (trans << 10u) | (face << 13u) | (ao << 16u) | (sun << 18u) | (torch << 24u));
+}
+
+} // namespace hc

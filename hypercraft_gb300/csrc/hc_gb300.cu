@@ -1,0 +1,401 @@
+// Kernels and the C ABI of the GB300 chunk relighter + mesher (include/hc_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/hc_gb300.h"
+#include "hc_mesh.cuh"
+#include "hc_registry.h"
+
+namespace hc {
+
+struct Refs27 {
+	const uint16_t *blk[27];
+	const int8_t *hgt[27];
+};
+
+__device__ __forceinline__ Smem &smem() {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	return *reinterpret_cast<Smem *>(smem_raw);
+}
+
+// One chunk, one CTA: the plain per-chunk form.
+__global__ void __launch_bounds__(kThreads, 1) k_mesh_single(Refs27 refs, DevTables T, Arena A) {
+	Smem &S = smem();
+	if (threadIdx.x < 27) {
+		S.blk[threadIdx.x] = refs.blk[threadIdx.x];
+		S.hgt[threadIdx.x] = refs.hgt[threadIdx.x];
+	}
+	__syncthreads();
+	mesh_chunk_cta(S, T, A, 0);
+}
+
+// Relight only, writing the 34^3 region the mesher reads.
+__global__ void __launch_bounds__(kThreads, 1) k_relight_single(Refs27 refs, DevTables T, uint8_t *light34) {
+	Smem &S = smem();
+	if (threadIdx.x < 27) {
+		S.blk[threadIdx.x] = refs.blk[threadIdx.x];
+		S.hgt[threadIdx.x] = refs.hgt[threadIdx.x];
+	}
+	for (int i = threadIdx.x; i < 256; i += kThreads)
+		S.classes[i] = T.classes[i];
+	__syncthreads();
+	relight_window(S, T);
+	__syncthreads();
+	for (int i = threadIdx.x; i < kLtCells; i += kThreads)
+		light34[i] = S.light[i];
+}
+
+} // namespace hc
+
+using namespace hc;
+
+struct hc_ctx {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	uint8_t *d_class_of = nullptr;
+	DevClass *d_classes = nullptr;
+	// single-chunk staging and output
+	uint16_t *d_blocks = nullptr;
+	int8_t *d_heights = nullptr;
+	uint16_t *h_blocks = nullptr; // pinned
+	int8_t *h_heights = nullptr;  // pinned
+	uint2 *d_verts = nullptr;
+	uint16_t *d_idx = nullptr;
+	hc_mesh_desc *d_meshes = nullptr;
+	unsigned long long *d_cursor = nullptr; // [0] quads, [1] meshes (as unsigned int in the low word)
+	uint32_t *d_results = nullptr;
+	uint32_t *h_results = nullptr; // pinned, 8 words
+	size_t smem_bytes = 0;
+	std::string err;
+};
+
+namespace {
+
+hc_status fail(hc_ctx *ctx, hc_status s, const std::string &msg) {
+	if (ctx)
+		ctx->err = msg;
+	return s;
+}
+
+#define HC_CUDA(ctx, call)                                                                                                 \
+	do {                                                                                                                   \
+		cudaError_t e_ = (call);                                                                                           \
+		if (e_ != cudaSuccess)                                                                                             \
+			return fail(ctx, e_ == cudaErrorMemoryAllocation ? HC_ERR_OUT_OF_MEMORY : HC_ERR_CUDA,                         \
+			            std::string(#call) + ": " + cudaGetErrorString(e_));                                               \
+	} while (0)
+
+// Derives the block classes from the registry: each distinct device row gets one id.
+bool build_classes(const hc_registry &reg, std::vector<uint8_t> &class_of, std::vector<DevClass> &classes) {
+	class_of.assign(65536, 0);
+	classes.clear();
+	std::map<std::string, uint8_t> seen;
+	for (uint32_t raw = 0; raw < 65536u; ++raw) {
+		const hc_block_props &p = reg.props[raw];
+		DevClass d;
+		std::memset(&d, 0, sizeof(d));
+		bool all_empty = true, all_opaque = true;
+		for (int f = 0; f < 6; ++f) {
+			d.tex[f] = p.tex[f];
+			const bool empty = (p.tex[f] & 0x1fffu) == 0;
+			all_empty &= empty;
+			all_opaque &= !empty && !hc_tex_is_transparent(p.tex[f]);
+		}
+		const bool vertical = p.transparency == HC_TRANSPARENT;
+		uint8_t flags = 0;
+		if (p.transparency != HC_OPAQUE)
+			flags |= kFIndirect;
+		if (vertical || p.collision != HC_COLLISION_SOLID)
+			flags |= kFDirect;
+		if (vertical)
+			flags |= kFVertical;
+		if (p.mesh_kind == HC_MESH_NONE && all_opaque)
+			flags |= kFOpaqueCube;
+		if (p.mesh_kind == HC_MESH_NONE && all_empty)
+			flags |= kFEmpty;
+		const uint8_t tag = p.id == HC_BLK_AIR ? kTagAir
+		                    : p.id == HC_BLK_WATER ? kTagSource
+		                    : p.id == HC_BLK_FLOWING_WATER ? kTagFlow
+		                                                   : kTagOther;
+		flags |= (uint8_t)(tag << kFTagShift);
+		d.flags = flags;
+		d.light = p.light_level;
+		d.mesh_first = p.mesh_kind == HC_MESH_STATIC ? p.mesh_first : 0;
+		const uint8_t param = p.mesh_kind == HC_MESH_STATIC ? p.mesh_count : (p.mesh_kind == HC_MESH_FLOW ? p.flow_variant : 0);
+		d.mesh_meta = (uint8_t)(p.mesh_kind | (param << 2));
+		std::string key(reinterpret_cast<const char *>(&d), sizeof(d));
+		auto it = seen.find(key);
+		if (it == seen.end()) {
+			if (classes.size() >= 256)
+				return false;
+			it = seen.emplace(key, (uint8_t)classes.size()).first;
+			classes.push_back(d);
+		}
+		class_of[raw] = it->second;
+	}
+	classes.resize(256, classes[0]);
+	return true;
+}
+
+hc_status upload_tables(hc_ctx *ctx) {
+	static hc_registry reg; // 1.3 MB; built once per process
+	static bool built = false;
+	if (!built) {
+		hc_registry_build(&reg);
+		built = true;
+	}
+	std::vector<uint8_t> class_of;
+	std::vector<DevClass> classes;
+	if (!build_classes(reg, class_of, classes))
+		return fail(ctx, HC_ERR_INVALID_ARG, "more than 256 distinct block classes");
+	if (reg.static_face_count > HC_MAX_STATIC_FACES / 4)
+		return fail(ctx, HC_ERR_INVALID_ARG, "too many static custom-mesh faces");
+	uint64_t tt = 0, tl = 0, tp = 0;
+	for (int t = 0; t < HC_TEX_COUNT; ++t) {
+		tt |= (uint64_t)hc_tex_is_transparent((uint16_t)t) << t;
+		tl |= (uint64_t)hc_tex_is_liquid((uint16_t)t) << t;
+		tp |= (uint64_t)hc_tex_use_transparent_pass((uint16_t)t) << t;
+	}
+	HC_CUDA(ctx, cudaMalloc(&ctx->d_class_of, 65536));
+	HC_CUDA(ctx, cudaMalloc(&ctx->d_classes, 256 * sizeof(DevClass)));
+	HC_CUDA(ctx, cudaMemcpy(ctx->d_class_of, class_of.data(), 65536, cudaMemcpyHostToDevice));
+	HC_CUDA(ctx, cudaMemcpy(ctx->d_classes, classes.data(), 256 * sizeof(DevClass), cudaMemcpyHostToDevice));
+	HC_CUDA(ctx, cudaMemcpyToSymbol(c_tex_transparent, &tt, sizeof(tt)));
+	HC_CUDA(ctx, cudaMemcpyToSymbol(c_tex_liquid, &tl, sizeof(tl)));
+	HC_CUDA(ctx, cudaMemcpyToSymbol(c_tex_transpass, &tp, sizeof(tp)));
+	HC_CUDA(ctx, cudaMemcpyToSymbol(c_static_faces, reg.static_faces, sizeof(hc_mesh_face) * reg.static_face_count));
+	return HC_OK;
+}
+
+DevTables tables(const hc_ctx *ctx) { return DevTables{ctx->d_class_of, ctx->d_classes}; }
+
+hc_status check_refs(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27]) {
+	if (!blocks || !heights)
+		return fail(ctx, HC_ERR_INVALID_ARG, "null neighbour array");
+	for (int i = 0; i < 27; ++i)
+		if (!blocks[i] || !heights[i])
+			return fail(ctx, HC_ERR_INVALID_ARG, "null chunk pointer at neighbour " + std::to_string(i));
+	return HC_OK;
+}
+
+// Runs the single-chunk kernel into the given device buffers; reads back the 5 result words.
+hc_status run_single(hc_ctx *ctx, const Refs27 &refs, uint2 *verts, uint16_t *idx, hc_mesh_desc *meshes,
+                     unsigned long long quad_cap, unsigned int mesh_cap, cudaStream_t st) {
+	HC_CUDA(ctx, cudaMemsetAsync(ctx->d_cursor, 0, 2 * sizeof(unsigned long long), st));
+	Arena A{verts, idx, meshes, ctx->d_cursor, reinterpret_cast<unsigned int *>(ctx->d_cursor + 1), quad_cap, mesh_cap,
+	        ctx->d_results};
+	k_mesh_single<<<1, kThreads, ctx->smem_bytes, st>>>(refs, tables(ctx), A);
+	HC_CUDA(ctx, cudaGetLastError());
+	HC_CUDA(ctx, cudaMemcpyAsync(ctx->h_results, ctx->d_results, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	return HC_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *hc_status_string(hc_status s) {
+	switch (s) {
+	case HC_OK:
+		return "ok";
+	case HC_ERR_INVALID_ARG:
+		return "invalid argument";
+	case HC_ERR_OUT_OF_MEMORY:
+		return "out of memory";
+	case HC_ERR_CAPACITY:
+		return "output capacity exceeded";
+	case HC_ERR_DEVICE_TIMEOUT:
+		return "device wait timed out";
+	case HC_ERR_CUDA:
+		return "CUDA error";
+	case HC_ERR_NO_DEVICE:
+		return "no usable device";
+	}
+	return "unknown status";
+}
+
+const char *hc_last_error(const hc_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+hc_status hc_ctx_create(int device, hc_ctx **out) {
+	if (!out)
+		return HC_ERR_INVALID_ARG;
+	*out = nullptr;
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+		return HC_ERR_NO_DEVICE;
+	hc_ctx *ctx = new hc_ctx();
+	ctx->device = device;
+	hc_status s = HC_OK;
+	do {
+		if (cudaSetDevice(device) != cudaSuccess) {
+			s = fail(ctx, HC_ERR_NO_DEVICE, "cudaSetDevice failed");
+			break;
+		}
+		cudaDeviceProp prop;
+		if (cudaGetDeviceProperties(&prop, device) != cudaSuccess || prop.major < 10) {
+			s = fail(ctx, HC_ERR_NO_DEVICE, "device is not a Blackwell-class GPU");
+			break;
+		}
+		ctx->smem_bytes = sizeof(Smem);
+		if (cudaFuncSetAttribute(k_mesh_single, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes) !=
+		        cudaSuccess ||
+		    cudaFuncSetAttribute(k_relight_single, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes) !=
+		        cudaSuccess) {
+			s = fail(ctx, HC_ERR_NO_DEVICE, "cannot reserve " + std::to_string(ctx->smem_bytes) + " B of shared memory");
+			break;
+		}
+		if ((s = upload_tables(ctx)) != HC_OK)
+			break;
+		const auto chk = [&](cudaError_t e, const char *what) {
+			if (e != cudaSuccess && s == HC_OK)
+				s = fail(ctx, e == cudaErrorMemoryAllocation ? HC_ERR_OUT_OF_MEMORY : HC_ERR_CUDA,
+				         std::string(what) + ": " + cudaGetErrorString(e));
+		};
+		chk(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream");
+		chk(cudaMalloc(&ctx->d_blocks, 27 * 32768 * sizeof(uint16_t)), "blocks");
+		chk(cudaMalloc(&ctx->d_heights, 27 * 1024), "heights");
+		chk(cudaMallocHost(&ctx->h_blocks, 27 * 32768 * sizeof(uint16_t)), "pinned blocks");
+		chk(cudaMallocHost(&ctx->h_heights, 27 * 1024), "pinned heights");
+		chk(cudaMalloc(&ctx->d_verts, (size_t)HC_CHUNK_MAX_QUADS * 4 * sizeof(uint2)), "vertices");
+		chk(cudaMalloc(&ctx->d_idx, (size_t)HC_CHUNK_MAX_QUADS * 6 * sizeof(uint16_t)), "indices");
+		chk(cudaMalloc(&ctx->d_meshes, HC_CHUNK_MAX_MESHES * sizeof(hc_mesh_desc)), "meshes");
+		chk(cudaMalloc(&ctx->d_cursor, 2 * sizeof(unsigned long long)), "cursor");
+		chk(cudaMalloc(&ctx->d_results, 8 * sizeof(uint32_t)), "results");
+		chk(cudaMallocHost(&ctx->h_results, 8 * sizeof(uint32_t)), "pinned results");
+	} while (0);
+	if (s != HC_OK) {
+		std::fprintf(stderr, "hc_ctx_create: %s\n", ctx->err.c_str());
+		hc_ctx_destroy(ctx);
+		return s;
+	}
+	*out = ctx;
+	return HC_OK;
+}
+
+void hc_ctx_destroy(hc_ctx *ctx) {
+	if (!ctx)
+		return;
+	cudaSetDevice(ctx->device);
+	cudaFree(ctx->d_class_of);
+	cudaFree(ctx->d_classes);
+	cudaFree(ctx->d_blocks);
+	cudaFree(ctx->d_heights);
+	cudaFreeHost(ctx->h_blocks);
+	cudaFreeHost(ctx->h_heights);
+	cudaFree(ctx->d_verts);
+	cudaFree(ctx->d_idx);
+	cudaFree(ctx->d_meshes);
+	cudaFree(ctx->d_cursor);
+	cudaFree(ctx->d_results);
+	cudaFreeHost(ctx->h_results);
+	if (ctx->stream)
+		cudaStreamDestroy(ctx->stream);
+	delete ctx;
+}
+
+hc_status hc_mesh_chunk(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27], hc_chunk_mesh *out,
+                        void *stream) {
+	if (!ctx || !out)
+		return HC_ERR_INVALID_ARG;
+	hc_status s = check_refs(ctx, blocks, heights);
+	if (s != HC_OK)
+		return s;
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	for (int i = 0; i < 27; ++i) {
+		std::memcpy(ctx->h_blocks + (size_t)i * 32768, blocks[i], 32768 * sizeof(uint16_t));
+		std::memcpy(ctx->h_heights + (size_t)i * 1024, heights[i], 1024);
+	}
+	HC_CUDA(ctx, cudaMemcpyAsync(ctx->d_blocks, ctx->h_blocks, 27 * 32768 * sizeof(uint16_t), cudaMemcpyHostToDevice, st));
+	HC_CUDA(ctx, cudaMemcpyAsync(ctx->d_heights, ctx->h_heights, 27 * 1024, cudaMemcpyHostToDevice, st));
+	Refs27 refs;
+	for (int i = 0; i < 27; ++i) {
+		refs.blk[i] = ctx->d_blocks + (size_t)i * 32768;
+		refs.hgt[i] = ctx->d_heights + (size_t)i * 1024;
+	}
+	if ((s = run_single(ctx, refs, ctx->d_verts, ctx->d_idx, ctx->d_meshes, HC_CHUNK_MAX_QUADS, HC_CHUNK_MAX_MESHES, st)) !=
+	    HC_OK)
+		return s;
+	const uint32_t *r = ctx->h_results;
+	const uint32_t q = r[0] + r[1];
+	out->mesh_count = r[3];
+	out->vertex_count = 4 * q;
+	out->index_count = 6 * q;
+	if (r[4] != kChunkOk)
+		return fail(ctx, HC_ERR_CAPACITY, "chunk exceeds the single-chunk output buffers");
+	if (out->mesh_count > out->mesh_capacity || out->vertex_count > out->vertex_capacity ||
+	    out->index_count > out->index_capacity)
+		return fail(ctx, HC_ERR_CAPACITY, "caller output buffers too small");
+	if (out->mesh_count && (!out->meshes || !out->vertices || !out->indices))
+		return fail(ctx, HC_ERR_INVALID_ARG, "null output buffer");
+	if (out->mesh_count) {
+		HC_CUDA(ctx, cudaMemcpyAsync(out->meshes, ctx->d_meshes, out->mesh_count * sizeof(hc_mesh_desc),
+		                             cudaMemcpyDeviceToHost, st));
+		HC_CUDA(ctx, cudaMemcpyAsync(out->vertices, ctx->d_verts, (size_t)out->vertex_count * sizeof(uint2),
+		                             cudaMemcpyDeviceToHost, st));
+		HC_CUDA(ctx, cudaMemcpyAsync(out->indices, ctx->d_idx, (size_t)out->index_count * sizeof(uint16_t),
+		                             cudaMemcpyDeviceToHost, st));
+		HC_CUDA(ctx, cudaStreamSynchronize(st));
+	}
+	return HC_OK;
+}
+
+hc_status hc_mesh_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27],
+                               hc_chunk_mesh *out, void *stream) {
+	if (!ctx || !out)
+		return HC_ERR_INVALID_ARG;
+	hc_status s = check_refs(ctx, blocks, heights);
+	if (s != HC_OK)
+		return s;
+	if (!out->meshes || !out->vertices || !out->indices)
+		return fail(ctx, HC_ERR_INVALID_ARG, "null output buffer");
+	if ((reinterpret_cast<uintptr_t>(out->vertices) & 15u) || (reinterpret_cast<uintptr_t>(out->indices) & 3u))
+		return fail(ctx, HC_ERR_INVALID_ARG, "vertices must be 16-byte and indices 4-byte aligned");
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	Refs27 refs;
+	for (int i = 0; i < 27; ++i) {
+		refs.blk[i] = blocks[i];
+		refs.hgt[i] = heights[i];
+	}
+	const unsigned long long qcap = std::min(out->vertex_capacity / 4, out->index_capacity / 6);
+	if ((s = run_single(ctx, refs, reinterpret_cast<uint2 *>(out->vertices), out->indices, out->meshes, qcap,
+	                    out->mesh_capacity, st)) != HC_OK)
+		return s;
+	const uint32_t *r = ctx->h_results;
+	const uint32_t q = r[0] + r[1];
+	out->mesh_count = r[3];
+	out->vertex_count = 4 * q;
+	out->index_count = 6 * q;
+	if (r[4] != kChunkOk)
+		return fail(ctx, HC_ERR_CAPACITY, "caller output buffers too small");
+	return HC_OK;
+}
+
+hc_status hc_relight_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27],
+                                  uint8_t *light34, void *stream) {
+	if (!ctx || !light34)
+		return HC_ERR_INVALID_ARG;
+	hc_status s = check_refs(ctx, blocks, heights);
+	if (s != HC_OK)
+		return s;
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	Refs27 refs;
+	for (int i = 0; i < 27; ++i) {
+		refs.blk[i] = blocks[i];
+		refs.hgt[i] = heights[i];
+	}
+	k_relight_single<<<1, kThreads, ctx->smem_bytes, st>>>(refs, tables(ctx), light34);
+	HC_CUDA(ctx, cudaGetLastError());
+	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	return HC_OK;
+}
+
+} // extern "C"

@@ -10,6 +10,7 @@
 //   cactus ............... block/block/cactus.hpp:4-48
 //   liquid flow mesh ..... block/block/public/Liquid.hpp:266-417, Water.hpp:5-14
 #include "hc_registry.h"
+#include "hc_flow.h"
 
 #include <initializer_list>
 #include <string.h>
@@ -318,72 +319,7 @@ int hc_registry_build(hc_registry *reg) {
 
 void hc_flow_mesh(const uint16_t nei[8], uint8_t variant, hc_mesh_face *faces, uint32_t *face_count,
                   uint16_t textures[6]) {
-	const uint16_t kFlowTex = HC_TEX_WATER, kNone = HC_TEX_NONE;
-	const auto nei_height = [](uint16_t raw) -> int8_t {
-		unsigned id = raw & 0xffu;
-		if (id == HC_BLK_WATER)
-			return 16;
-		if (id == HC_BLK_FLOWING_WATER) {
-			unsigned h = (raw >> 8) * 2u;
-			return (int8_t)(uint8_t)(h > 1u ? h : 1u);
-		}
-		return id != HC_BLK_AIR ? -1 : 0;
-	};
-	int8_t nh[8];
-	for (int i = 0; i < 8; ++i)
-		nh[i] = nei_height(nei[i]);
-	const int8_t nb = (int8_t)(uint8_t)(variant * 2u > 1u ? variant * 2u : 1u);
-	const auto vh = [&](int a, int b, int c) -> uint8_t {
-		int8_t m1 = nb > nh[a] ? nb : nh[a];
-		int8_t m2 = nh[b] > nh[c] ? nh[b] : nh[c];
-		uint8_t mx = (uint8_t)(m1 > m2 ? m1 : m2);
-		if (mx != 16 && (nb == 0) + (nh[a] == 0) + (nh[b] == 0) + (nh[c] == 0) >= 3)
-			return 0;
-		return mx;
-	};
-	const uint8_t h0 = vh(0, 1, 3), h1 = vh(1, 2, 4), h2 = vh(3, 5, 6), h3 = vh(4, 6, 7);
-	const auto is_liquid = [](uint16_t raw) {
-		unsigned id = raw & 0xffu;
-		return id == HC_BLK_WATER || id == HC_BLK_FLOWING_WATER;
-	};
-	if (h0 == 16 && h1 == 16 && h2 == 16 && h3 == 16) {
-		*face_count = 0;
-		for (int i = 0; i < 6; ++i)
-			textures[i] = kFlowTex;
-		return;
-	}
-	uint32_t n = 0;
-	{
-		const int v[4][3] = {{0, h0, 0}, {0, h2, 16}, {16, h3, 16}, {16, h1, 0}};
-		faces[n++] = face(1, HC_FACE_TOP, HC_FACE_TOP, kFlowTex, v);
-	}
-	const bool left_full = h0 == 16 && h2 == 16, left_empty = h0 == 0 && h2 == 0;
-	const bool right_full = h1 == 16 && h3 == 16, right_empty = h1 == 0 && h3 == 0;
-	const bool front_full = h2 == 16 && h3 == 16, front_empty = h2 == 0 && h3 == 0;
-	const bool back_full = h0 == 16 && h1 == 16, back_empty = h0 == 0 && h1 == 0;
-	if (!left_full && !left_empty && !is_liquid(nei[3])) {
-		const int v[4][3] = {{0, h0, 0}, {0, 0, 0}, {0, 0, 16}, {0, h2, 16}};
-		faces[n++] = face(0, HC_FACE_LEFT, HC_FACE_LEFT, kFlowTex, v);
-	}
-	if (!right_full && !right_empty && !is_liquid(nei[4])) {
-		const int v[4][3] = {{16, 0, 0}, {16, h1, 0}, {16, h3, 16}, {16, 0, 16}};
-		faces[n++] = face(0, HC_FACE_RIGHT, HC_FACE_RIGHT, kFlowTex, v);
-	}
-	if (!back_full && !back_empty && !is_liquid(nei[1])) {
-		const int v[4][3] = {{0, 0, 0}, {0, h0, 0}, {16, h1, 0}, {16, 0, 0}};
-		faces[n++] = face(2, HC_FACE_BACK, HC_FACE_BACK, kFlowTex, v);
-	}
-	if (!front_full && !front_empty && !is_liquid(nei[6])) {
-		const int v[4][3] = {{0, h2, 16}, {0, 0, 16}, {16, 0, 16}, {16, h3, 16}};
-		faces[n++] = face(2, HC_FACE_FRONT, HC_FACE_FRONT, kFlowTex, v);
-	}
-	*face_count = n;
-	textures[HC_FACE_TOP] = HC_TEX_NONE;
-	textures[HC_FACE_LEFT] = left_full ? kFlowTex : kNone;
-	textures[HC_FACE_RIGHT] = right_full ? kFlowTex : kNone;
-	textures[HC_FACE_FRONT] = front_full ? kFlowTex : kNone;
-	textures[HC_FACE_BACK] = back_full ? kFlowTex : kNone;
-	textures[HC_FACE_BOTTOM] = kFlowTex;
+	hc_flow_mesh_impl(nei, variant, faces, face_count, textures);
 }
 
 } // extern "C"

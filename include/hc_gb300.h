@@ -1,0 +1,105 @@
+/* GB300 chunk relighter + mesher for HyperCraft: the C ABI.
+ *
+ * This library replaces the body of the client's per-chunk mesh task,
+ *   ChunkTaskRunner<ChunkTaskType::kMesh>::Run   (client/src/ChunkMeshTask.cpp:41-127),
+ * i.e. the 62^3 light-window seed (lines 49-87), the sun and torch flood fills
+ * BlockLightAlgo::PropagateLight (lines 89-111, client/include/client/BlockLightAlgo.hpp:44-73) and
+ * BlockMeshAlgo::Generate (lines 113-122, client/include/client/BlockMeshAlgo.hpp:494-521).
+ * Its output is the std::vector<BlockMesh> that WorldRenderer::PushChunkMesh consumes
+ * (client/include/client/WorldRenderer.hpp:69-87), byte for byte: the same packed 8-byte vertices
+ * (client/include/client/BlockVertex.hpp:8-18), uint16 indices, per-mesh uint32 AABBs, transparent
+ * flags, mesh split at 65,532 vertices and mesh order.
+ *
+ * Inputs follow the reference's chunk layout (client/include/client/Chunk.hpp:95-96): a chunk is
+ * 32^3 uint16 blocks (raw = id | meta << 8, index x + (y*32 + z)*32) and 32^2 int8 sunlight heights
+ * (index x + z*32). A call takes the 27 chunks of a neighbourhood in the reference's neighbour order
+ * (common/include/common/Position.hpp:138-152; the centre chunk is index 26).
+ *
+ * All entry points return an hc_status. Pointers are plain host or device pointers; no type from
+ * any framework appears here. A context is bound to one CUDA device; calls on one context from
+ * several threads must use distinct streams.
+ */
+#ifndef HC_GB300_H
+#define HC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum hc_status {
+	HC_OK = 0,
+	HC_ERR_INVALID_ARG = 1,    /* null pointer, bad size or bad slot */
+	HC_ERR_OUT_OF_MEMORY = 2,  /* device or pinned allocation failed */
+	HC_ERR_CAPACITY = 3,       /* an output buffer is too small; the required sizes are written back */
+	HC_ERR_DEVICE_TIMEOUT = 4, /* a bounded device-side wait gave up */
+	HC_ERR_CUDA = 5,           /* a CUDA runtime call failed; see hc_last_error */
+	HC_ERR_NO_DEVICE = 6       /* no usable sm_103 device, or the kernels are not loadable */
+} hc_status;
+
+typedef struct hc_ctx hc_ctx;
+typedef struct hc_pool hc_pool;
+
+/* One mesh of the output, in reference order. Offsets count elements (vertices of 8 bytes, uint16
+ * indices) from the start of the vertex / index buffer the call wrote. Index values are local to
+ * the mesh, as in the reference. 48 bytes. */
+typedef struct hc_mesh_desc {
+	uint32_t vertex_offset;
+	uint32_t vertex_count;
+	uint32_t index_offset;
+	uint32_t index_count;
+	uint32_t aabb_min[3]; /* 1/16-voxel units, UINT32_MAX when empty (dep/AABB.hpp:11) */
+	uint32_t aabb_max[3];
+	uint32_t transparent; /* 1 for the transparent-pass stream */
+	uint32_t chunk;       /* batch position of the chunk (0 for single-chunk calls) */
+} hc_mesh_desc;
+
+/* Output of a single-chunk call. The caller sets the three capacities and the three pointers
+ * (host pointers for hc_mesh_chunk, device pointers for hc_mesh_chunk_device); the call writes
+ * the counts. On HC_ERR_CAPACITY the counts hold the required sizes and nothing else is valid.
+ * Vertices are two uint32 words each (x10_y10_z10_axis2, tex10_trans3_face3_ao2_sl6_tl6). */
+typedef struct hc_chunk_mesh {
+	uint32_t mesh_capacity, vertex_capacity, index_capacity;
+	uint32_t mesh_count, vertex_count, index_count;
+	hc_mesh_desc *meshes;
+	uint32_t *vertices;
+	uint16_t *indices;
+} hc_chunk_mesh;
+
+/* Worst case of one chunk: 720,896 quads (custom + regular faces), 45 meshes per stream. */
+#define HC_CHUNK_MAX_QUADS 720896u
+#define HC_CHUNK_MAX_MESHES 96u
+
+const char *hc_status_string(hc_status s);
+/* Text of the last error on this context (empty if none). */
+const char *hc_last_error(const hc_ctx *ctx);
+
+/* Creates a context on CUDA device `device`: uploads the block tables and allocates the
+ * single-chunk staging and output buffers. */
+hc_status hc_ctx_create(int device, hc_ctx **out);
+void hc_ctx_destroy(hc_ctx *ctx);
+
+/* Drop-in for ChunkMeshTask.cpp:48-122 with host buffers: copies the 27 chunks to the device,
+ * relights the centre chunk's window, meshes it and copies the meshes back into `out` (host
+ * pointers). `stream` is a cudaStream_t (NULL = the context's own stream). Synchronous. */
+hc_status hc_mesh_chunk(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27],
+                        hc_chunk_mesh *out, void *stream);
+
+/* Same computation with every pointer on the device (blocks[i], heights[i] and out's three
+ * buffers). Enqueues on `stream` and waits only to read the counts back. */
+hc_status hc_mesh_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27],
+                               hc_chunk_mesh *out, void *stream);
+
+/* Relight only: the 34^3 light region the mesher reads ([-1, 32]^3 of the centre chunk; index
+ * (x+1) + ((z+1) + (y+1)*34)*34; sun in the low nibble, torch in the high nibble), as produced by
+ * the window flood fill of ChunkMeshTask.cpp:48-111. Device pointers throughout. */
+hc_status hc_relight_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27],
+                                  uint8_t *light34, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HC_GB300_H */
