@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Benchmark of the chunk relight + mesh path on one GB300 (or N replicas under torchrun).
+
+A step relights and meshes every chunk of the scale workload: 32 x 8 x 32 = 8,192 chunks of seeded
+value-noise terrain with caves and glowstone (plus a ring of lit all-air chunks so each has 26
+neighbours), resident in the device chunk pool. The timed form is the batched persistent
+work-stealing kernel replayed as a CUDA graph; the plain one-launch-per-chunk form is timed beside
+it. Output is byte-identical to the reference (tests/); a sample is re-checked here.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload scale|mixture] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+DESC_BYTES = 48
+RESULT_BYTES = 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="scale", choices=["scale", "mixture"])
+    ap.add_argument("--size", default="", help="override grid as NXxNYxNZ (profiling runs)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the per-chunk form (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dims(args):
+    if args.size:
+        return tuple(int(x) for x in args.size.lower().split("x"))
+    return (32, 8, 32) if args.workload == "scale" else (32, 16, 32)
+
+
+def make_world(args, rank):
+    from hypercraft_gb300 import worldgen
+    nx, ny, nz = dims(args)
+    seed = worldgen.WORLD_SEED + 7919 * rank
+    if args.workload == "scale":
+        return worldgen.scale_world(nx, ny, nz, seed=seed)
+    return worldgen.mixture_world(nx, ny, nz, seed=seed)
+
+
+def workload_name(args):
+    nx, ny, nz = dims(args)
+    if args.workload == "scale":
+        return (f"scale: {nx}x{ny}x{nz}={nx * ny * nz} chunks of seeded 2D value-noise terrain with 3D value-noise "
+                f"caves (~15% of underground) and 2% glowstone torches, 5% leaves, ring of lit air chunks")
+    return (f"mixture: {nx}x{ny}x{nz}={nx * ny * nz} chunks, seeded 30% air / 20% stone / 35% terrain / "
+            f"10% random fill / 5% checkerboard, shuffled, ring of lit air chunks")
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_run(world_obj, chunks, nbr, runner, threads):
+    from oracle import bind
+    t0 = time.perf_counter()
+    q, m = bind.mesh_many(runner, world_obj.blocks, world_obj.heights, nbr, threads)
+    return time.perf_counter() - t0, q, m
+
+
+def reference_arm(args):
+    """The reference's CPU path on the host cores: oracle/_ref where it was built from the reference
+    sources here, else the CPU restatement (oracle/hc_oracle.cpp)."""
+    from oracle import bind
+    rank, world, _ = dist_setup(args)
+    if rank != 0:
+        return
+    import __graft_entry__  # noqa: F401
+    from hypercraft_gb300.build import build
+    build()
+    ref = bind.reference()
+    runner, kind = (ref, "reference") if ref is not None else (bind.oracle(), "port")
+    w = make_world(args, 0)
+    chunks = w.meshable()
+    nbr = w.neighbour_table(chunks)
+    threads = os.cpu_count()
+    sample = min(len(chunks), 2048)
+    rng = np.random.default_rng(1)
+    times, quads = [], 0
+    for step in range(args.warmup + args.steps):
+        pick = np.sort(rng.choice(len(chunks), sample, replace=False))
+        dt, q, _ = cpu_run(w, chunks[pick], nbr[pick], runner, threads)
+        if step >= args.warmup:
+            times.append(dt)
+            quads += q
+    total = sum(times)
+    value = sample * args.steps / total
+    line = {
+        "impl": "reference", "metric": "chunks/s", "value": value, "unit": "chunks/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic",
+        "config": {"workload": workload_name(args), "sample_chunks_per_step": sample},
+        "quads_per_s": quads / total,
+        "cpu_baseline": {"value": value, "unit": "chunks/s", "cores": threads, "kind": kind,
+                         "sample": f"{sample} random chunks of the workload per step, {threads} threads"},
+        "e2e": {"value": value, "unit": "chunks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def ours(args):
+    import torch
+    rank, world, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from hypercraft_gb300.build import build
+    if rank == 0:
+        build()
+    barrier(world)
+    from hypercraft_gb300 import batch, mesher
+
+    ctx = mesher.Context(local)
+    w = make_world(args, rank)
+    rw = batch.upload_world(ctx, w)
+    n = len(rw.chunks)
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes_stream(stream)
+
+    # size the arena from a counting run, then allocate it with a margin
+    probe = batch.Arena(1, 1, n, local)
+    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, probe, batch.PERSISTENT)
+    plan.launch(sp)
+    need_q, need_m, _ = plan.result(check=False)
+    plan.close()
+    arena = batch.Arena(int(need_q * 1.05) + 1024, int(need_m * 1.05) + 64, n, local)
+    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, batch.PERSISTENT)
+
+    for _ in range(args.warmup):
+        plan.launch(sp)
+    quads, meshes, failed = plan.result()
+    assert failed == 0, f"{failed} chunks failed"
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.launch(sp)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    ms_total = ev0.elapsed_time(ev1)
+    q2, m2, f2 = plan.result()
+    assert (q2, m2, f2) == (quads, meshes, 0)
+    ms_total = max_over_ranks(ms_total, world, dev)
+    chunks_all = sum_over_ranks(n * args.steps, world, dev)
+    quads_all = sum_over_ranks(quads * args.steps, world, dev)
+    value = chunks_all / (ms_total / 1e3)
+    ms_step = ms_total / args.steps
+
+    algo_bytes = n * (65536 + 1024 + RESULT_BYTES) + 44 * quads + DESC_BYTES * meshes
+    peak, peak_kind = hbm_peak()
+    achieved = algo_bytes / (ms_step / 1e3) / 1e9
+
+    # plain form: one kernel launch per chunk, same arena layout
+    plain_value = None
+    plain_checked = None
+    if not args.no_plain:
+        parena = batch.Arena(arena.quad_capacity, arena.mesh_capacity, n, local)
+        pplan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, parena, batch.PER_CHUNK)
+        pplan.launch(sp)
+        pplan.result()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        pplan.launch(sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pq, pm, pf = pplan.result()
+        plain_value = n / (e0.elapsed_time(e1) / 1e3)
+        # byte-exact check of a sample of chunks between the two forms
+        hb, hp = arena.host(), parena.host()
+        rng = np.random.default_rng(3)
+        sample = rng.choice(n, min(n, 256), replace=False)
+        plain_checked = (pq, pm, pf) == (quads, meshes, 0) and all(
+            a == b for i in sample for a, b in zip(arena.chunk_meshes(int(i), hb), parena.chunk_meshes(int(i), hp)))
+        assert plain_checked, "batched and per-chunk forms differ"
+        pplan.close()
+        del parena
+
+    # end to end through the C ABI with host buffers: upload the world from pinned memory, mesh,
+    # read every quad, mesh descriptor and per-chunk result back to pinned memory
+    e2e = None
+    if not args.no_e2e:
+        hb = torch.from_numpy(w.blocks.view(np.int16)).pin_memory()
+        hh = torch.from_numpy(w.heights).pin_memory()
+        out_v = torch.empty(quads * 8, dtype=torch.int32).pin_memory()
+        out_i = torch.empty(quads * 6, dtype=torch.int16).pin_memory()
+        out_d = torch.empty(meshes * 12, dtype=torch.int32).pin_memory()
+        out_r = torch.empty(n * 5, dtype=torch.int32).pin_memory()
+        lib = rw.pool.lib
+
+        def e2e_step():
+            ctx.check(lib.hc_pool_upload(rw.pool.handle, 0, w.n_chunks, hb.data_ptr(), hh.data_ptr(), 0, sp), "upload")
+            plan.launch(sp)
+            q, m, f = plan.result()
+            ctx.check(lib.hc_batch_plan_download(plan.handle, q, m, out_v.data_ptr(), out_i.data_ptr(),
+                                                 out_d.data_ptr(), out_r.data_ptr()), "download")
+            return q, m
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        t_e2e = max_over_ranks(time.perf_counter() - t0, world, dev)
+        e2e = {"value": chunks_all / t_e2e, "unit": "chunks/s",
+               "h2d_bytes_per_step": int(w.n_chunks * (65536 + 1024)),
+               "d2h_bytes_per_step": int(quads * 44 + meshes * DESC_BYTES + n * RESULT_BYTES)}
+
+    cpu = None
+    if rank == 0 and world >= 1 and not args.no_cpu:
+        from oracle import bind
+        sample = min(n, 2048)
+        threads = os.cpu_count()
+        dt, q, _ = cpu_run(w, rw.chunks[:sample], rw.neighbours[:sample], bind.oracle(), threads)
+        cpu = {"value": sample / dt, "unit": "chunks/s", "cores": threads, "kind": "port",
+               "sample": f"first {sample} of the {n} workload chunks, {threads} threads, {q} quads"}
+
+    if rank == 0:
+        nx, ny, nz = dims(args)
+        line = {
+            "metric": "chunks/s", "value": value, "unit": "chunks/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u16",
+            "data": "synthetic: seeded worlds generated in-process (the reference publishes no benchmark data)",
+            "config": {"workload": workload_name(args), "chunks_per_gpu": n, "form": "batched persistent "
+                       "work-stealing kernel, CUDA graph", "parallelism": f"replicas x{world}",
+                       "l2": f"inputs larger than L2: pool {w.n_chunks * 66560 / 1e6:.0f} MB, output "
+                             f"{(44 * quads) / 1e6:.0f} MB per step"},
+            "quads_per_s": quads_all / (ms_total / 1e3),
+            "quads_per_step": quads, "meshes_per_step": meshes,
+            "plain_chunks_per_s": plain_value,
+            "batched_vs_plain": (value / world / plain_value) if plain_value else None,
+            "byte_exact_vs_plain_sample": plain_checked,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_source": f"{peak_kind} ({'MEASURED_PEAKS.json hbm_gbs' if peak_kind == 'measured' else 'fallback'})",
+                         "algorithmic_bytes_per_launch": algo_bytes},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def ctypes_stream(stream):
+    import ctypes
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

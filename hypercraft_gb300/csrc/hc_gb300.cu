@@ -50,9 +50,103 @@ __global__ void __launch_bounds__(kThreads, 1) k_relight_single(Refs27 refs, Dev
 		light34[i] = S.light[i];
 }
 
+enum : uint32_t { kChunkBadSlot = 2 };
+
+// Points S.blk / S.hgt at the 27 neighbour slots of batch item `item`; false if a slot is invalid.
+__device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *pool_heights, uint32_t pool_cap,
+                          const int32_t *nbr, uint32_t item) {
+	__shared__ int s_bad;
+	if (threadIdx.x == 0)
+		s_bad = 0;
+	__syncthreads();
+	if (threadIdx.x < 27) {
+		const int32_t slot = nbr[(size_t)item * 27 + threadIdx.x];
+		if (slot < 0 || (uint32_t)slot >= pool_cap) {
+			s_bad = 1;
+			S.blk[threadIdx.x] = pool_blocks;
+			S.hgt[threadIdx.x] = pool_heights;
+		} else {
+			S.blk[threadIdx.x] = pool_blocks + (size_t)slot * 32768;
+			S.hgt[threadIdx.x] = pool_heights + (size_t)slot * 1024;
+		}
+	}
+	__syncthreads();
+	return s_bad == 0;
+}
+
+__device__ void bad_item(const Arena &A, uint32_t item, unsigned int *failed) {
+	if (threadIdx.x == 0) {
+		uint32_t *r = A.results + 5 * (size_t)item;
+		r[0] = r[1] = r[2] = r[3] = 0;
+		r[4] = kChunkBadSlot;
+		atomicAdd(failed, 1u);
+	}
+}
+
+// Batched form: a persistent grid; each CTA takes the next chunk from a device work counter.
+__global__ void __launch_bounds__(kThreads, 1)
+    k_mesh_batch(const uint16_t *pool_blocks, const int8_t *pool_heights, uint32_t pool_cap, const int32_t *nbr, uint32_t n,
+                 unsigned int *work, unsigned int *failed, DevTables T, Arena A) {
+	Smem &S = smem();
+	__shared__ uint32_t s_item;
+	for (;;) {
+		if (threadIdx.x == 0)
+			s_item = atomicAdd(work, 1u);
+		__syncthreads();
+		const uint32_t item = s_item;
+		if (item >= n)
+			break;
+		if (load_refs(S, pool_blocks, pool_heights, pool_cap, nbr, item)) {
+			mesh_chunk_cta(S, T, A, item);
+			if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
+				atomicAdd(failed, 1u);
+		} else {
+			bad_item(A, item, failed);
+		}
+		__syncthreads();
+	}
+}
+
+// Plain form at scale: one launch per chunk.
+__global__ void __launch_bounds__(kThreads, 1)
+    k_mesh_item(const uint16_t *pool_blocks, const int8_t *pool_heights, uint32_t pool_cap, const int32_t *nbr, uint32_t item,
+                unsigned int *failed, DevTables T, Arena A) {
+	Smem &S = smem();
+	if (load_refs(S, pool_blocks, pool_heights, pool_cap, nbr, item)) {
+		mesh_chunk_cta(S, T, A, item);
+		if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
+			atomicAdd(failed, 1u);
+	} else {
+		bad_item(A, item, failed);
+	}
+}
+
 } // namespace hc
 
 using namespace hc;
+
+struct hc_pool {
+	hc_ctx *ctx = nullptr;
+	uint32_t capacity = 0;
+	uint16_t *d_blocks = nullptr;
+	int8_t *d_heights = nullptr;
+};
+
+struct hc_batch_plan {
+	hc_ctx *ctx = nullptr;
+	hc_pool *pool = nullptr;
+	const int32_t *nbr = nullptr;
+	uint32_t n = 0;
+	hc_batch_arena arena{};
+	int mode = HC_BATCH_PERSISTENT;
+	int grid = 0;
+	unsigned long long *d_state = nullptr; // quad cursor, mesh cursor, work counter, failed chunks
+	unsigned long long *h_state = nullptr; // pinned
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	cudaStream_t capture_stream = nullptr;
+	cudaStream_t last = nullptr;
+};
 
 struct hc_ctx {
 	int device = 0;
@@ -246,6 +340,10 @@ hc_status hc_ctx_create(int device, hc_ctx **out) {
 		if (cudaFuncSetAttribute(k_mesh_single, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes) !=
 		        cudaSuccess ||
 		    cudaFuncSetAttribute(k_relight_single, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes) !=
+		        cudaSuccess ||
+		    cudaFuncSetAttribute(k_mesh_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes) !=
+		        cudaSuccess ||
+		    cudaFuncSetAttribute(k_mesh_item, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes) !=
 		        cudaSuccess) {
 			s = fail(ctx, HC_ERR_NO_DEVICE, "cannot reserve " + std::to_string(ctx->smem_bytes) + " B of shared memory");
 			break;
@@ -394,6 +492,223 @@ hc_status hc_relight_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27],
 	}
 	k_relight_single<<<1, kThreads, ctx->smem_bytes, st>>>(refs, tables(ctx), light34);
 	HC_CUDA(ctx, cudaGetLastError());
+	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	return HC_OK;
+}
+
+hc_status hc_pool_create(hc_ctx *ctx, uint32_t capacity, hc_pool **out) {
+	if (!ctx || !out || capacity == 0)
+		return HC_ERR_INVALID_ARG;
+	*out = nullptr;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	hc_pool *p = new hc_pool();
+	p->ctx = ctx;
+	p->capacity = capacity;
+	cudaError_t e = cudaMalloc(&p->d_blocks, (size_t)capacity * 32768 * sizeof(uint16_t));
+	if (e == cudaSuccess)
+		e = cudaMalloc(&p->d_heights, (size_t)capacity * 1024);
+	if (e != cudaSuccess) {
+		hc_pool_destroy(p);
+		return fail(ctx, e == cudaErrorMemoryAllocation ? HC_ERR_OUT_OF_MEMORY : HC_ERR_CUDA,
+		            std::string("pool allocation: ") + cudaGetErrorString(e));
+	}
+	*out = p;
+	return HC_OK;
+}
+
+void hc_pool_destroy(hc_pool *pool) {
+	if (!pool)
+		return;
+	cudaSetDevice(pool->ctx->device);
+	cudaFree(pool->d_blocks);
+	cudaFree(pool->d_heights);
+	delete pool;
+}
+
+uint32_t hc_pool_capacity(const hc_pool *pool) { return pool ? pool->capacity : 0; }
+
+hc_status hc_pool_buffers(const hc_pool *pool, uint16_t **blocks, int8_t **heights) {
+	if (!pool || !blocks || !heights)
+		return HC_ERR_INVALID_ARG;
+	*blocks = pool->d_blocks;
+	*heights = pool->d_heights;
+	return HC_OK;
+}
+
+hc_status hc_pool_upload(hc_pool *pool, uint32_t first, uint32_t count, const uint16_t *blocks, const int8_t *heights,
+                         int src_on_device, void *stream) {
+	if (!pool || !blocks || !heights)
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = pool->ctx;
+	if ((uint64_t)first + count > pool->capacity)
+		return fail(ctx, HC_ERR_INVALID_ARG, "upload beyond the pool capacity");
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	const cudaMemcpyKind kind = src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	HC_CUDA(ctx, cudaMemcpyAsync(pool->d_blocks + (size_t)first * 32768, blocks, (size_t)count * 32768 * sizeof(uint16_t),
+	                             kind, st));
+	HC_CUDA(ctx, cudaMemcpyAsync(pool->d_heights + (size_t)first * 1024, heights, (size_t)count * 1024, kind, st));
+	return HC_OK;
+}
+
+namespace {
+
+Arena plan_arena(const hc_batch_plan *p) {
+	return Arena{reinterpret_cast<uint2 *>(p->arena.vertices),
+	             p->arena.indices,
+	             p->arena.meshes,
+	             p->d_state,
+	             reinterpret_cast<unsigned int *>(p->d_state + 1),
+	             p->arena.quad_capacity,
+	             p->arena.mesh_capacity,
+	             p->arena.results};
+}
+
+hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
+	hc_ctx *ctx = p->ctx;
+	HC_CUDA(ctx, cudaMemsetAsync(p->d_state, 0, 4 * sizeof(unsigned long long), st));
+	const Arena A = plan_arena(p);
+	unsigned int *work = reinterpret_cast<unsigned int *>(p->d_state + 2);
+	unsigned int *failed = reinterpret_cast<unsigned int *>(p->d_state + 3);
+	if (p->mode == HC_BATCH_PERSISTENT) {
+		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(p->pool->d_blocks, p->pool->d_heights, p->pool->capacity,
+		                                                          p->nbr, p->n, work, failed, tables(ctx), A);
+		HC_CUDA(ctx, cudaGetLastError());
+	} else {
+		for (uint32_t i = 0; i < p->n; ++i) {
+			k_mesh_item<<<1, kThreads, ctx->smem_bytes, st>>>(p->pool->d_blocks, p->pool->d_heights, p->pool->capacity,
+			                                                  p->nbr, i, failed, tables(ctx), A);
+		}
+		HC_CUDA(ctx, cudaGetLastError());
+	}
+	return HC_OK;
+}
+
+} // namespace
+
+hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighbours, uint32_t n,
+                               const hc_batch_arena *arena, int mode, int ctas_per_sm, hc_batch_plan **out) {
+	if (!ctx || !pool || !neighbours || !arena || !out || n == 0 || !arena->vertices || !arena->indices ||
+	    !arena->meshes || !arena->results)
+		return HC_ERR_INVALID_ARG;
+	if (mode != HC_BATCH_PERSISTENT && mode != HC_BATCH_PER_CHUNK)
+		return fail(ctx, HC_ERR_INVALID_ARG, "unknown batch mode");
+	if ((reinterpret_cast<uintptr_t>(arena->vertices) & 15u) || (reinterpret_cast<uintptr_t>(arena->indices) & 3u))
+		return fail(ctx, HC_ERR_INVALID_ARG, "vertices must be 16-byte and indices 4-byte aligned");
+	if (arena->quad_capacity > 0xffffffffull / 6)
+		return fail(ctx, HC_ERR_INVALID_ARG, "quad capacity exceeds the 32-bit index offsets");
+	*out = nullptr;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	hc_batch_plan *p = new hc_batch_plan();
+	p->ctx = ctx;
+	p->pool = pool;
+	p->nbr = neighbours;
+	p->n = n;
+	p->arena = *arena;
+	p->mode = mode;
+	int sms = 0, per_sm = 0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mesh_batch, kThreads, ctx->smem_bytes);
+	if (per_sm < 1)
+		per_sm = 1;
+	if (ctas_per_sm > 0 && ctas_per_sm < per_sm)
+		per_sm = ctas_per_sm;
+	p->grid = sms * per_sm;
+	hc_status s = HC_OK;
+	cudaError_t e = cudaMalloc(&p->d_state, 4 * sizeof(unsigned long long));
+	if (e == cudaSuccess)
+		e = cudaMallocHost(&p->h_state, 4 * sizeof(unsigned long long));
+	if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT) {
+		e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
+		if (e == cudaSuccess)
+			e = cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal);
+		if (e == cudaSuccess) {
+			s = enqueue_plan(p, p->capture_stream);
+			cudaError_t e2 = cudaStreamEndCapture(p->capture_stream, &p->graph);
+			if (s == HC_OK)
+				e = e2;
+		}
+		if (e == cudaSuccess && s == HC_OK)
+			e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+	}
+	if (e != cudaSuccess || s != HC_OK) {
+		if (s == HC_OK)
+			s = fail(ctx, e == cudaErrorMemoryAllocation ? HC_ERR_OUT_OF_MEMORY : HC_ERR_CUDA,
+			         std::string("batch plan: ") + cudaGetErrorString(e));
+		hc_batch_plan_destroy(p);
+		return s;
+	}
+	*out = p;
+	return HC_OK;
+}
+
+void hc_batch_plan_destroy(hc_batch_plan *plan) {
+	if (!plan)
+		return;
+	cudaSetDevice(plan->ctx->device);
+	if (plan->exec)
+		cudaGraphExecDestroy(plan->exec);
+	if (plan->graph)
+		cudaGraphDestroy(plan->graph);
+	if (plan->capture_stream)
+		cudaStreamDestroy(plan->capture_stream);
+	cudaFree(plan->d_state);
+	cudaFreeHost(plan->h_state);
+	delete plan;
+}
+
+hc_status hc_batch_plan_launch(hc_batch_plan *plan, void *stream) {
+	if (!plan)
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = plan->ctx;
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	plan->last = st;
+	if (plan->exec) {
+		HC_CUDA(ctx, cudaGraphLaunch(plan->exec, st));
+		return HC_OK;
+	}
+	return enqueue_plan(plan, st);
+}
+
+hc_status hc_batch_plan_result(hc_batch_plan *plan, uint64_t *quads, uint32_t *meshes, uint32_t *failed_chunks) {
+	if (!plan)
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = plan->ctx;
+	cudaStream_t st = plan->last ? plan->last : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	HC_CUDA(ctx, cudaMemcpyAsync(plan->h_state, plan->d_state, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	if (quads)
+		*quads = plan->h_state[0];
+	if (meshes)
+		*meshes = (uint32_t)(plan->h_state[1] & 0xffffffffu);
+	if (failed_chunks)
+		*failed_chunks = (uint32_t)(plan->h_state[3] & 0xffffffffu);
+	return (plan->h_state[0] > plan->arena.quad_capacity || (plan->h_state[1] & 0xffffffffu) > plan->arena.mesh_capacity)
+	           ? fail(ctx, HC_ERR_CAPACITY, "batch arena too small")
+	           : HC_OK;
+}
+
+hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t meshes, uint32_t *vertices,
+                                 uint16_t *indices, hc_mesh_desc *mesh_descs, uint32_t *results) {
+	if (!plan)
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = plan->ctx;
+	if (quads > plan->arena.quad_capacity || meshes > plan->arena.mesh_capacity)
+		return fail(ctx, HC_ERR_INVALID_ARG, "download beyond the arena");
+	cudaStream_t st = plan->last ? plan->last : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	if (vertices && quads)
+		HC_CUDA(ctx, cudaMemcpyAsync(vertices, plan->arena.vertices, quads * 4 * sizeof(uint2), cudaMemcpyDeviceToHost, st));
+	if (indices && quads)
+		HC_CUDA(ctx, cudaMemcpyAsync(indices, plan->arena.indices, quads * 6 * sizeof(uint16_t), cudaMemcpyDeviceToHost, st));
+	if (mesh_descs && meshes)
+		HC_CUDA(ctx, cudaMemcpyAsync(mesh_descs, plan->arena.meshes, (size_t)meshes * sizeof(hc_mesh_desc),
+		                             cudaMemcpyDeviceToHost, st));
+	if (results)
+		HC_CUDA(ctx, cudaMemcpyAsync(results, plan->arena.results, (size_t)plan->n * 5 * sizeof(uint32_t),
+		                             cudaMemcpyDeviceToHost, st));
 	HC_CUDA(ctx, cudaStreamSynchronize(st));
 	return HC_OK;
 }

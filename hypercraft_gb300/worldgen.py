@@ -85,12 +85,16 @@ class World:
         return np.nonzero(ok)[0].astype(np.int32)
 
     def neighbour_table(self, chunks) -> np.ndarray:
-        """(len(chunks), 27) int32 neighbour table for the given chunk indices."""
-        chunks = np.asarray(chunks)
-        t = np.empty((len(chunks), 27), np.int32)
-        for k, c in enumerate(chunks):
-            t[k] = self.neighbours(*self.coords(int(c)))
-        return t
+        """(len(chunks), 27) int32 neighbour table for the given chunk indices (-1 outside the grid);
+        the same order as ``neighbours`` (common/include/common/Position.hpp:146-152)."""
+        c = np.asarray(chunks, np.int64)
+        ix, iz, iy = c % self.nx, (c // self.nx) % self.nz, c // (self.nx * self.nz)
+        rev = np.array([1, -1, 0])
+        i = np.arange(27)
+        dx, dy, dz = rev[i // 9], rev[(i // 3) % 3], rev[i % 3]
+        x, y, z = ix[:, None] + dx, iy[:, None] + dy, iz[:, None] + dz
+        ok = (x >= 0) & (y >= 0) & (z >= 0) & (x < self.nx) & (y < self.ny) & (z < self.nz)
+        return np.where(ok, x + self.nx * (z + self.nz * y), -1).astype(np.int32)
 
     def recompute_heights(self, threads: int = 0) -> None:
         _load().hcw_recompute_heights(ctypes.byref(self._grid()), self.kinds.ctypes.data, int(self.air_ring),

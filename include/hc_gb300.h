@@ -98,6 +98,65 @@ hc_status hc_mesh_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27], co
 hc_status hc_relight_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27],
                                   uint8_t *light34, void *stream);
 
+
+/* ----------------------------------------------------------------------------------------------
+ * Device chunk pool and batched meshing.
+ *
+ * The reference meshes one chunk per worker-thread task (ChunkTaskPool::Run,
+ * client/src/ChunkTaskPool.cpp:87-130). Here chunks stay resident in a device pool of slots and
+ * a batch names, per chunk to mesh, its 27 neighbour slots (neighbour order, centre last). The
+ * batched form runs one persistent kernel whose CTAs take chunks from a device work counter;
+ * the plain form launches the single-chunk kernel once per chunk. Both write each chunk's meshes
+ * to the same arena layout, byte-identical to hc_mesh_chunk.
+ * ---------------------------------------------------------------------------------------------- */
+
+/* Creates a pool of `capacity` chunk slots (64 KiB of blocks + 1 KiB of heights each). */
+hc_status hc_pool_create(hc_ctx *ctx, uint32_t capacity, hc_pool **out);
+void hc_pool_destroy(hc_pool *pool);
+uint32_t hc_pool_capacity(const hc_pool *pool);
+/* Device base pointers of the pool (slot s at blocks + s*32768, heights + s*1024). */
+hc_status hc_pool_buffers(const hc_pool *pool, uint16_t **blocks, int8_t **heights);
+/* Copies `count` chunks into slots [first, first + count). `src_on_device` selects device or host
+ * sources. Asynchronous on `stream`. */
+hc_status hc_pool_upload(hc_pool *pool, uint32_t first, uint32_t count, const uint16_t *blocks, const int8_t *heights,
+                         int src_on_device, void *stream);
+
+/* Arena that receives a batch's meshes (all pointers on the device). Chunk i of the batch gets
+ * results[5*i .. 5*i+4] = {opaque quads, transparent quads, first mesh, mesh count, status}
+ * (status 0 = ok, 1 = arena full, 2 = bad neighbour slot); its meshes are meshes[first ..
+ * first + count), whose offsets index `vertices` / `indices`. The arena layout across chunks
+ * depends on scheduling; each chunk's meshes are byte-identical to hc_mesh_chunk. */
+typedef struct hc_batch_arena {
+	uint64_t quad_capacity; /* vertices hold 4 * quad_capacity, indices 6 * quad_capacity */
+	uint32_t mesh_capacity;
+	uint32_t *vertices;
+	uint16_t *indices;
+	hc_mesh_desc *meshes;
+	uint32_t *results;
+} hc_batch_arena;
+
+typedef struct hc_batch_plan hc_batch_plan;
+
+enum { HC_BATCH_PERSISTENT = 0, HC_BATCH_PER_CHUNK = 1 };
+
+/* Plans meshing `n` chunks whose neighbour slot table (n x 27 int32, device) is `neighbours`:
+ * mode HC_BATCH_PERSISTENT captures {cursor reset, persistent work-stealing kernel} as a CUDA
+ * graph; HC_BATCH_PER_CHUNK launches the single-chunk kernel once per chunk. `ctas_per_sm`
+ * (0 = automatic) sizes the persistent grid. */
+hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighbours, uint32_t n,
+                               const hc_batch_arena *arena, int mode, int ctas_per_sm, hc_batch_plan **out);
+void hc_batch_plan_destroy(hc_batch_plan *plan);
+/* Enqueues one run of the plan on `stream` (NULL = the context stream). */
+hc_status hc_batch_plan_launch(hc_batch_plan *plan, void *stream);
+/* Waits for the last launch and reads the arena cursors: quads and meshes written (or required,
+ * when some chunk reported a full arena) and the number of chunks with a non-zero status. */
+hc_status hc_batch_plan_result(hc_batch_plan *plan, uint64_t *quads, uint32_t *meshes, uint32_t *failed_chunks);
+/* Copies the last run's output to host memory: the first `quads` quads of the arena (4 vertices
+ * of 2 uint32 words and 6 uint16 indices each), `meshes` descriptors and the n x 5 result words.
+ * Any destination may be NULL to skip it. Synchronous. */
+hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t meshes, uint32_t *vertices,
+                                 uint16_t *indices, hc_mesh_desc *mesh_descs, uint32_t *results);
+
 #ifdef __cplusplus
 }
 #endif

@@ -148,7 +148,24 @@ def reference() -> _Runner | None:
     return _reference
 
 
+def _bind_many(lib, name):
+    f = getattr(lib, name)
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p]
+    f.restype = ctypes.c_uint64
+
+
+def mesh_many(runner, blocks: np.ndarray, heights: np.ndarray, nbr: np.ndarray, threads: int):
+    """Relights + meshes every row of the (n, 27) chunk-index table `nbr` on `threads` threads;
+    returns (quads, meshes)."""
+    nbr = np.ascontiguousarray(nbr, np.int32)
+    m = ctypes.c_uint64()
+    fn = getattr(runner.lib, runner.prefix + "_mesh_many")
+    q = fn(blocks.ctypes.data, heights.ctypes.data, nbr.ctypes.data, nbr.shape[0], threads, ctypes.byref(m))
+    return int(q), int(m.value)
+
+
 def _bind_oracle_extras(lib):
+    _bind_many(lib, "hco_mesh_many")
     lib.hco_mesh_chunk_lit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(FlatMeshes)]
     lib.hco_dump_registry.argtypes = [ctypes.c_void_p] * 9
     lib.hco_flow_mesh.argtypes = [ctypes.c_void_p, ctypes.c_uint8, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
@@ -156,6 +173,7 @@ def _bind_oracle_extras(lib):
 
 
 def _bind_reference_extras(lib):
+    _bind_many(lib, "hcref_mesh_many")
     lib.hcref_dump_registry.argtypes = [ctypes.c_void_p] * 6 + [ctypes.c_uint32, ctypes.c_void_p]
     lib.hcref_flow_mesh.argtypes = [ctypes.c_uint16, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     lib.hcref_flow_fetch_offsets.argtypes = [ctypes.c_uint16, ctypes.c_void_p, ctypes.c_void_p]

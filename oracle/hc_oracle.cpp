@@ -18,7 +18,9 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <deque>
+#include <thread>
 #include <vector>
 
 #include "../hypercraft_gb300/csrc/hc_registry.h"
@@ -394,8 +396,8 @@ struct Mesher {
 
 	// BlockMeshAlgo.hpp:308-482
 	void regular_axis(int axis) {
-		static uint16_t tex_mask[2][1024]; // persists across slices like the reference's locals
-		static Light4 light_mask[2][1024];
+		thread_local uint16_t tex_mask[2][1024]; // persists across slices like the reference's locals
+		thread_local Light4 light_mask[2][1024];
 		std::memset(tex_mask, 0, sizeof(tex_mask));
 		const int u_axis = axis == 1 ? 2 : 1, v_axis = axis == 0 ? 2 : 0;
 		const bool uv_cycle = (u_axis + 1) % 3 == v_axis;
@@ -583,5 +585,43 @@ void hco_flow_mesh(const uint16_t *nei8, uint8_t variant, uint8_t *faces_out, ui
 
 // ChunkShouldRemesh (client/include/client/ChunkMeshTask.inl:9-15).
 int hco_chunk_should_remesh(int x, int y, int z) { return border_interfere(x, y, z, 15) ? 1 : 0; }
+
+// Meshes n chunks of a resident world (chunk c at blocks + c*32768, heights + c*1024; nbr holds 27
+// chunk indices per item) on `threads` threads, each with its own window and mesher state, the way
+// the reference's worker threads each own a runner. Returns the total quad count.
+uint64_t hco_mesh_many(const uint16_t *blocks, const int8_t *heights, const int32_t *nbr, uint32_t n, int threads,
+                       uint64_t *meshes_out) {
+	std::atomic<uint32_t> next{0};
+	std::atomic<uint64_t> quads{0}, meshes{0};
+	const auto work = [&] {
+		std::vector<uint8_t> window((size_t)kExt * kExt * kExt);
+		const uint16_t *b27[27];
+		const int8_t *h27[27];
+		for (uint32_t i; (i = next.fetch_add(1)) < n;) {
+			for (int k = 0; k < 27; ++k) {
+				b27[k] = blocks + (size_t)nbr[(size_t)i * 27 + k] * 32768;
+				h27[k] = heights + (size_t)nbr[(size_t)i * 27 + k] * 1024;
+			}
+			World27 w{b27, h27};
+			relight_window(w, window.data());
+			Mesher m(w, window.data());
+			m.generate();
+			uint64_t q = 0;
+			for (const auto &mesh : m.meshes)
+				q += mesh.vertex_count() / 4;
+			quads += q;
+			meshes += m.meshes.size();
+		}
+	};
+	std::vector<std::thread> ts;
+	for (int t = 1; t < threads; ++t)
+		ts.emplace_back(work);
+	work();
+	for (auto &t : ts)
+		t.join();
+	if (meshes_out)
+		*meshes_out = meshes;
+	return quads;
+}
 
 } // extern "C"

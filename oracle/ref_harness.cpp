@@ -9,7 +9,9 @@
 #include <client/BlockMeshAlgo.hpp>
 #include <common/Position.hpp>
 
+#include <atomic>
 #include <cstring>
+#include <thread>
 #include <map>
 #include <vector>
 
@@ -267,6 +269,41 @@ int hcref_flow_fetch_offsets(uint16_t self_raw, int8_t *xyz, uint32_t *count) {
 // IsBorderLightInterfere at level 15; the .inl itself includes the renderer, so it is called here.
 int hcref_chunk_should_remesh(int x, int y, int z) {
 	return LightAlgo::IsBorderLightInterfere((InnerPos1)x, (InnerPos1)y, (InnerPos1)z, 15) ? 1 : 0;
+}
+
+// Same driver as the oracle's hco_mesh_many, over the reference's own templates.
+uint64_t hcref_mesh_many(const uint16_t *blocks, const int8_t *heights, const int32_t *nbr, uint32_t n, int threads,
+                         uint64_t *meshes_out) {
+	std::atomic<uint32_t> next{0};
+	std::atomic<uint64_t> quads{0}, meshes{0};
+	const auto work = [&] {
+		const uint16_t *b27[27];
+		const int8_t *h27[27];
+		Runner &r = runner();
+		for (uint32_t i; (i = next.fetch_add(1)) < n;) {
+			for (int k = 0; k < 27; ++k) {
+				b27[k] = blocks + (size_t)nbr[(size_t)i * 27 + k] * 32768;
+				h27[k] = heights + (size_t)nbr[(size_t)i * 27 + k] * 1024;
+			}
+			Neighbours nb{b27, h27};
+			r.relight(nb);
+			auto ms = r.mesh(nb);
+			uint64_t q = 0;
+			for (const auto &m : ms)
+				q += m.vertices.size() / 4;
+			quads += q;
+			meshes += ms.size();
+		}
+	};
+	std::vector<std::thread> ts;
+	for (int t = 1; t < threads; ++t)
+		ts.emplace_back(work);
+	work();
+	for (auto &t : ts)
+		t.join();
+	if (meshes_out)
+		*meshes_out = meshes;
+	return quads;
 }
 
 } // extern "C"
