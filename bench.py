@@ -228,7 +228,9 @@ def ours(args):
     w = make_world(args, rank)
     rw = batch.upload_world(ctx, w)
     n = len(rw.chunks)
-    stream = torch.cuda.current_stream(dev)
+    # all work (library calls and timing events) on one dedicated non-default stream
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     sp = ctypes_stream(stream)
 
     # size the arena from a counting run, then allocate it with a margin

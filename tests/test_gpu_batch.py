@@ -1,0 +1,86 @@
+"""Batched forms (persistent work-stealing kernel in a CUDA graph, and one launch per chunk) give
+each chunk exactly the meshes of the single-chunk call and of the CPU oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_world(kind):
+    from hypercraft_gb300 import worldgen
+    return worldgen.scale_world(4, 3, 4) if kind == "scale" else worldgen.mixture_world(4, 4, 4)
+
+
+@pytest.mark.parametrize("kind", ["scale", "mixture"])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_batch_matches_oracle(ctx, oracle, kind, mode):
+    from hypercraft_gb300 import batch
+    w = _small_world(kind)
+    rw = batch.upload_world(ctx, w)
+    n = len(rw.chunks)
+    arena = batch.Arena(3_000_000, 4096, n)
+    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, mode)
+    for _ in range(2):  # replay: cursors and work counter reset each launch
+        plan.launch()
+        q, m, f = plan.result()
+    assert f == 0
+    host = arena.host()
+    total = 0
+    for i, c in enumerate(rw.chunks):
+        got = arena.chunk_meshes(i, host)
+        nb = rw.neighbours[i]
+        want = oracle.mesh_chunk([w.blocks[k] for k in nb], [w.heights[k] for k in nb])
+        assert len(got) == len(want), (i, int(c))
+        assert all(a == b for a, b in zip(got, want)), (i, int(c))
+        total += sum(len(x.vertices) for x in got) // 4
+    assert total == q
+
+
+def test_batch_matches_single_chunk_call(ctx):
+    from hypercraft_gb300 import batch
+    w = _small_world("mixture")
+    rw = batch.upload_world(ctx, w)
+    arena = batch.Arena(3_000_000, 4096, len(rw.chunks))
+    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, batch.PERSISTENT, ctas_per_sm=1)
+    plan.launch()
+    plan.result()
+    host = arena.host()
+    for i in range(0, len(rw.chunks), 5):
+        nb = rw.neighbours[i]
+        single = ctx.mesh_chunk([w.blocks[k] for k in nb], [w.heights[k] for k in nb])
+        got = arena.chunk_meshes(i, host)
+        assert len(got) == len(single) and all(a == b for a, b in zip(got, single))
+
+
+def test_bad_neighbour_slot_is_reported(ctx):
+    from hypercraft_gb300 import batch
+    w = _small_world("scale")
+    rw = batch.upload_world(ctx, w)
+    nbr = rw.neighbours.copy()
+    nbr[1, 3] = -1
+    nbr[2, 26] = w.n_chunks + 5
+    arena = batch.Arena(3_000_000, 4096, len(nbr))
+    plan = batch.BatchPlan(ctx, rw.pool, nbr, arena, batch.PERSISTENT)
+    plan.launch()
+    q, m, f = plan.result()
+    assert f == 2
+    res = arena.host()["results"].reshape(-1, 5)
+    assert res[1, 4] == batch.RESULT_BAD_SLOT and res[2, 4] == batch.RESULT_BAD_SLOT
+    assert (res[[0] + list(range(3, len(nbr))), 4] == 0).all()
+
+
+def test_small_arena_reports_capacity(ctx):
+    from hypercraft_gb300 import batch
+    from hypercraft_gb300.mesher import HcError, HC_ERR_CAPACITY
+    w = _small_world("mixture")
+    rw = batch.upload_world(ctx, w)
+    arena = batch.Arena(1000, 8, len(rw.chunks))
+    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, batch.PERSISTENT)
+    plan.launch()
+    with pytest.raises(HcError) as e:
+        plan.result()
+    assert e.value.status == HC_ERR_CAPACITY
+    q, m, f = plan.result(check=False)
+    assert q > 1000 and f > 0  # required sizes are reported; chunks that did not fit are flagged
+    res = arena.host()["results"].reshape(-1, 5)
+    assert ((res[:, 4] == 0) | (res[:, 4] == batch.RESULT_ARENA_FULL)).all()
