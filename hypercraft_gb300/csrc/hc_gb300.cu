@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -714,3 +715,229 @@ hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t m
 }
 
 } // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// Meshing without device allocation.
+//
+// Some callers cannot call cudaMalloc: code that runs inside a host application's render or frame
+// loop under a fixed device-memory budget, or a plugin whose host owns every device allocation. For
+// them hc_mesh_batch_noalloc runs the batched kernel with its scratch (arena cursors, work counter,
+// failed-chunk count and the five result words per chunk) and its block tables in file-scope
+// device arrays below. Every GPU that loads this library holds them (about 390 KB) until exit.
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t kNoAllocMaxChunks = HC_NOALLOC_MAX_CHUNKS;
+constexpr uint32_t kNoAllocStateWords = 8; // quad cursor (u64), mesh cursor (u64), work counter, failed count
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocStateWords + 5 * kNoAllocMaxChunks];
+static __device__ __align__(256) uint8_t g_noalloc_class_of[65536];
+static __device__ __align__(256) DevClass g_noalloc_classes[256];
+
+constexpr int kNoAllocMaxDevices = 64;
+struct NoAllocDevice {
+	bool ready;
+	int sms;
+	uint32_t *scratch;
+	uint8_t *class_of;
+	DevClass *classes;
+};
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+std::mutex g_noalloc_mutex;
+
+// Host copies of the tables, in static storage (no heap).
+hc_registry g_noalloc_registry;
+uint8_t g_noalloc_class_of_host[65536];
+DevClass g_noalloc_classes_host[256];
+bool g_noalloc_tables_built = false;
+
+DevClass noalloc_class_row(const hc_block_props &p) {
+	DevClass d;
+	std::memset(&d, 0, sizeof(d));
+	bool all_empty = true, all_opaque = true;
+	for (int f = 0; f < 6; ++f) {
+		d.tex[f] = p.tex[f];
+		const bool empty = (p.tex[f] & 0x1fffu) == 0;
+		all_empty &= empty;
+		all_opaque &= !empty && !hc_tex_is_transparent(p.tex[f]);
+	}
+	const bool vertical = p.transparency == HC_TRANSPARENT;
+	uint8_t flags = 0;
+	if (p.transparency != HC_OPAQUE)
+		flags |= kFIndirect;
+	if (vertical || p.collision != HC_COLLISION_SOLID)
+		flags |= kFDirect;
+	if (vertical)
+		flags |= kFVertical;
+	if (p.mesh_kind == HC_MESH_NONE && all_opaque)
+		flags |= kFOpaqueCube;
+	if (p.mesh_kind == HC_MESH_NONE && all_empty)
+		flags |= kFEmpty;
+	const uint8_t tag = p.id == HC_BLK_AIR             ? kTagAir
+	                    : p.id == HC_BLK_WATER         ? kTagSource
+	                    : p.id == HC_BLK_FLOWING_WATER ? kTagFlow
+	                                                   : kTagOther;
+	d.flags = (uint8_t)(flags | (tag << kFTagShift));
+	d.light = p.light_level;
+	d.mesh_first = p.mesh_kind == HC_MESH_STATIC ? p.mesh_first : 0;
+	const uint8_t param = p.mesh_kind == HC_MESH_STATIC ? p.mesh_count : (p.mesh_kind == HC_MESH_FLOW ? p.flow_variant : 0);
+	d.mesh_meta = (uint8_t)(p.mesh_kind | (param << 2));
+	return d;
+}
+
+bool noalloc_build_tables() {
+	if (g_noalloc_tables_built)
+		return true;
+	hc_registry_build(&g_noalloc_registry);
+	uint32_t n = 0;
+	for (uint32_t raw = 0; raw < 65536u; ++raw) {
+		const DevClass d = noalloc_class_row(g_noalloc_registry.props[raw]);
+		uint32_t c = 0;
+		while (c < n && std::memcmp(&g_noalloc_classes_host[c], &d, sizeof(d)) != 0)
+			++c;
+		if (c == n) {
+			if (n == 256)
+				return false;
+			g_noalloc_classes_host[n++] = d;
+		}
+		g_noalloc_class_of_host[raw] = (uint8_t)c;
+	}
+	for (uint32_t c = n; c < 256; ++c)
+		g_noalloc_classes_host[c] = g_noalloc_classes_host[0];
+	g_noalloc_tables_built = true;
+	return true;
+}
+
+// Writes a message into the caller's buffer (no heap use on any path of this entry point).
+void noalloc_error(char *text, size_t size, const char *fmt, const char *arg = "", unsigned long long a = 0,
+                   unsigned long long b = 0) {
+	if (text && size)
+		std::snprintf(text, size, fmt, arg, a, b);
+}
+
+// Once per device, with that device current: tables, kernel attribute, symbol addresses.
+hc_status noalloc_setup(int dev, char *err, size_t err_size) {
+	std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+	NoAllocDevice &D = g_noalloc_dev[dev];
+	if (D.ready)
+		return HC_OK;
+	if (!noalloc_build_tables()) {
+		noalloc_error(err, err_size, "%smore than 256 distinct block classes");
+		return HC_ERR_INVALID_ARG;
+	}
+	uint64_t tt = 0, tl = 0, tp = 0;
+	for (int t = 0; t < HC_TEX_COUNT; ++t) {
+		tt |= (uint64_t)hc_tex_is_transparent((uint16_t)t) << t;
+		tl |= (uint64_t)hc_tex_is_liquid((uint16_t)t) << t;
+		tp |= (uint64_t)hc_tex_use_transparent_pass((uint16_t)t) << t;
+	}
+	cudaError_t e = cudaFuncSetAttribute(k_mesh_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Smem));
+	if (e == cudaSuccess)
+		e = cudaMemcpyToSymbol(g_noalloc_class_of, g_noalloc_class_of_host, sizeof(g_noalloc_class_of_host));
+	if (e == cudaSuccess)
+		e = cudaMemcpyToSymbol(g_noalloc_classes, g_noalloc_classes_host, sizeof(g_noalloc_classes_host));
+	if (e == cudaSuccess)
+		e = cudaMemcpyToSymbol(c_tex_transparent, &tt, sizeof(tt));
+	if (e == cudaSuccess)
+		e = cudaMemcpyToSymbol(c_tex_liquid, &tl, sizeof(tl));
+	if (e == cudaSuccess)
+		e = cudaMemcpyToSymbol(c_tex_transpass, &tp, sizeof(tp));
+	if (e == cudaSuccess)
+		e = cudaMemcpyToSymbol(c_static_faces, g_noalloc_registry.static_faces,
+		                       sizeof(hc_mesh_face) * g_noalloc_registry.static_face_count);
+	// In host code the arrays' names are host-side stand-ins; the kernel gets their device addresses.
+	if (e == cudaSuccess)
+		e = cudaGetSymbolAddress((void **)&D.scratch, g_noalloc_scratch);
+	if (e == cudaSuccess)
+		e = cudaGetSymbolAddress((void **)&D.class_of, g_noalloc_class_of);
+	if (e == cudaSuccess)
+		e = cudaGetSymbolAddress((void **)&D.classes, g_noalloc_classes);
+	if (e == cudaSuccess)
+		e = cudaDeviceGetAttribute(&D.sms, cudaDevAttrMultiProcessorCount, dev);
+	if (e != cudaSuccess) {
+		noalloc_error(err, err_size, "no-alloc set-up: %s", cudaGetErrorString(e));
+		return HC_ERR_CUDA;
+	}
+	D.ready = true;
+	return HC_OK;
+}
+
+} // namespace
+
+extern "C" hc_status hc_mesh_batch_noalloc(const uint16_t *pool_blocks, const int8_t *pool_heights, uint32_t pool_capacity,
+                                           const int32_t *neighbours, uint32_t n, uint32_t *vertices, uint16_t *indices,
+                                           hc_mesh_desc *meshes, uint64_t quad_capacity, uint32_t mesh_capacity,
+                                           uint32_t *results_host, uint64_t *quads, uint32_t *mesh_count,
+                                           uint32_t *failed_chunks, void *stream, char *error_text,
+                                           size_t error_text_size) {
+	noalloc_error(error_text, error_text_size, "%s");
+	if (!pool_blocks || !pool_heights || !neighbours || !vertices || !indices || !meshes || pool_capacity == 0) {
+		noalloc_error(error_text, error_text_size, "%snull buffer or empty pool");
+		return HC_ERR_INVALID_ARG;
+	}
+	if (n == 0 || n > kNoAllocMaxChunks) {
+		noalloc_error(error_text, error_text_size, "%sbatch of %llu chunks: the no-alloc path takes 1..%llu chunks per call", "",
+		              (unsigned long long)n, (unsigned long long)kNoAllocMaxChunks);
+		return HC_ERR_CAPACITY;
+	}
+	if ((reinterpret_cast<uintptr_t>(vertices) & 15u) || (reinterpret_cast<uintptr_t>(indices) & 3u)) {
+		noalloc_error(error_text, error_text_size, "%svertices must be 16-byte and indices 4-byte aligned");
+		return HC_ERR_INVALID_ARG;
+	}
+	if (quad_capacity > 0xffffffffull / 6) {
+		noalloc_error(error_text, error_text_size, "%squad capacity exceeds the 32-bit index offsets");
+		return HC_ERR_INVALID_ARG;
+	}
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+		noalloc_error(error_text, error_text_size, "%sno current CUDA device");
+		return HC_ERR_NO_DEVICE;
+	}
+	hc_status s = noalloc_setup(dev, error_text, error_text_size);
+	if (s != HC_OK)
+		return s;
+	const NoAllocDevice &D = g_noalloc_dev[dev];
+	cudaStream_t st = (cudaStream_t)stream;
+	uint32_t *state = D.scratch;
+	uint32_t *results = D.scratch + kNoAllocStateWords;
+	// the array keeps the previous call's contents: the cursors and counters must start at zero
+	e = cudaMemsetAsync(state, 0, kNoAllocStateWords * sizeof(uint32_t), st);
+	if (e == cudaSuccess) {
+		Arena A{reinterpret_cast<uint2 *>(vertices),
+		        indices,
+		        meshes,
+		        reinterpret_cast<unsigned long long *>(state),
+		        state + 2,
+		        quad_capacity,
+		        mesh_capacity,
+		        results};
+		k_mesh_batch<<<D.sms, kThreads, sizeof(Smem), st>>>(pool_blocks, pool_heights, pool_capacity, neighbours, n,
+		                                                     state + 4, state + 5, DevTables{D.class_of, D.classes}, A);
+		e = cudaGetLastError();
+	}
+	uint32_t host_state[kNoAllocStateWords];
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(host_state, state, sizeof(host_state), cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess && results_host)
+		e = cudaMemcpyAsync(results_host, results, (size_t)n * 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(st);
+	if (e != cudaSuccess) {
+		noalloc_error(error_text, error_text_size, "no-alloc batch: %s", cudaGetErrorString(e));
+		return HC_ERR_CUDA;
+	}
+	uint64_t q;
+	std::memcpy(&q, host_state, sizeof(q));
+	if (quads)
+		*quads = q;
+	if (mesh_count)
+		*mesh_count = host_state[2];
+	if (failed_chunks)
+		*failed_chunks = host_state[5];
+	if (q > quad_capacity || host_state[2] > mesh_capacity) {
+		noalloc_error(error_text, error_text_size, "%soutput buffers too small; the required sizes are written back");
+		return HC_ERR_CAPACITY;
+	}
+	return HC_OK;
+}

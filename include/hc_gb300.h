@@ -157,6 +157,32 @@ hc_status hc_batch_plan_result(hc_batch_plan *plan, uint64_t *quads, uint32_t *m
 hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t meshes, uint32_t *vertices,
                                  uint16_t *indices, hc_mesh_desc *mesh_descs, uint32_t *results);
 
+
+/* ----------------------------------------------------------------------------------------------
+ * Batched meshing that allocates nothing. No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory (a host application's frame loop under a fixed
+ * device-memory budget, or a plugin whose host owns every allocation): the same batched kernel
+ * and output as hc_batch_plan_launch, with every input and output buffer passed in by the caller
+ * (chunk pool arrays, neighbour slot table, vertices, indices, mesh descriptors, all device
+ * memory) and no context. Its scratch (arena cursors, work counter and the five result words per
+ * chunk) and its block tables live in fixed device arrays of this library (about 390 KB per GPU,
+ * held until exit). It calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * Limit: 1..HC_NOALLOC_MAX_CHUNKS chunks per call; larger batches return HC_ERR_CAPACITY.
+ * The first call on a device (the current one) sets the tables up with synchronous copies: make it
+ * before any stream capture. All calls on a device share the scratch, so calls that overlap on the
+ * GPU race; run them in one stream or one at a time. Synchronous: it waits for its stream.
+ * results_host (n x 5 words, may be NULL) receives {opaque quads, transparent quads, first mesh,
+ * mesh count, status} per chunk; error_text (may be NULL) receives a message.
+ * ---------------------------------------------------------------------------------------------- */
+#define HC_NOALLOC_MAX_CHUNKS 16384u
+hc_status hc_mesh_batch_noalloc(const uint16_t *pool_blocks, const int8_t *pool_heights, uint32_t pool_capacity,
+                                const int32_t *neighbours, uint32_t n, uint32_t *vertices, uint16_t *indices,
+                                hc_mesh_desc *meshes, uint64_t quad_capacity, uint32_t mesh_capacity,
+                                uint32_t *results_host, uint64_t *quads, uint32_t *mesh_count,
+                                uint32_t *failed_chunks, void *stream, char *error_text, size_t error_text_size);
+
 #ifdef __cplusplus
 }
 #endif
