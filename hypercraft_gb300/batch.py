@@ -173,3 +173,17 @@ def upload_world(ctx: Context, world, chunks=None) -> ResidentWorld:
     pool.upload(0, world.blocks, world.heights)
     chunks = world.meshable() if chunks is None else np.asarray(chunks, np.int32)
     return ResidentWorld(world, pool, chunks, world.neighbour_table(chunks))
+
+
+def pool_download(pool: Pool, first: int, count: int):
+    """Blocks (count, 32768) uint16 and heights (count, 1024) int8 of slots [first, first+count)."""
+    lib = _bind(library())
+    if not hasattr(lib, "_dl_bound"):
+        lib.hc_pool_download.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        lib._dl_bound = True
+    b = np.empty((count, 32768), np.uint16)
+    h = np.empty((count, 1024), np.int8)
+    pool.ctx.check(lib.hc_pool_download(pool.handle, first, count, b.ctypes.data, h.ctypes.data, 0, None),
+                   "hc_pool_download")
+    return b, h

@@ -8,7 +8,8 @@
 
 namespace hc {
 
-constexpr int kThreads = 512;
+constexpr int kThreads = 1024;
+constexpr int kBlocksPerThread = 32768 / kThreads; // inner blocks per thread in the custom-mesh passes
 constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 32;
 constexpr int kQuadsPerMesh = 16383;       // 65,532 vertices: the uint16 split point (BlockMeshAlgo.hpp:274)
@@ -17,16 +18,23 @@ constexpr int kPlanes = 198;               // 3 axes x 33 slices x 2 face direct
 constexpr int kSlices = 99;
 constexpr int kSegments = kPlanes + 1;     // segment 0 = custom meshes, then the planes in output order
 
-// Staged block classes cover x, z in [-2, 33] and y in [-1, 32]: the mesher reads [-1, 32]^3 and
-// a flowing liquid on that ring looks one more cell out horizontally (Liquid.hpp:406-415).
-constexpr int kClsX = 36, kClsY = 34, kClsZ = 36;
-constexpr int kClsCells = kClsX * kClsY * kClsZ; // 44,064
+// Staged block classes cover [-1, 32]^3, the cells the mesher reads (a flowing liquid's extra
+// horizontal neighbours are read from the chunk data directly).
+constexpr int kCls = 34;
+constexpr int kClsCells = kCls * kCls * kCls; // 39,304
 // Light of [-1, 32]^3, the region the mesher reads.
 constexpr int kLt = 34;
 constexpr int kLtCells = kLt * kLt * kLt; // 39,304
 // The relight window [-15, 47)^3 as 62 x 62 rows of 62-bit words (bit = x + 15).
 constexpr int kWin = 62;
 constexpr int kWinRows = kWin * kWin; // 3,844
+// Per-chunk bit planes (pass, sun, level-15 emitters) as 32-bit rows (bit = x, row = z + 32 y),
+// plus a flag word (bit 0: the chunk holds an emitter of level 1..14).
+constexpr int kPlaneWords = 1024;
+constexpr int kPlaneStride = 3 * kPlaneWords + 32;
+enum { kPlanePass = 0, kPlaneSun = 1, kPlaneT15 = 2 };
+// Quad records staged for dense emission (two words each).
+constexpr int kQuadBuf = 4096;
 
 // One block class: a distinct property row of the registry (65,536 raw values map onto < 256).
 struct DevClass {
@@ -88,23 +96,30 @@ __constant__ int8_t c_corner[6][4][3][3] = {
      {{0, 1, -1}, {1, 1, -1}, {1, 0, -1}},
      {{0, -1, -1}, {1, -1, -1}, {1, 0, -1}}}};
 
-// Shared memory of one chunk CTA (about 192 KB: one CTA per SM).
+// Shared memory of one chunk CTA (about 215 KB: one CTA per SM).
 struct Relight {
-	uint64_t pass[kWinRows];    // blocks light may enter
-	uint64_t sun[kWinRows];     // current level set of the sun channel
-	uint64_t torch[kWinRows];   // current level set of the torch channel
+	uint64_t pass[kWinRows];   // blocks light may enter
+	ulonglong2 lit[kWinRows];  // current level set: .x sun, .y torch
 	uint32_t low_rows[(kWinRows + 31) / 32]; // rows holding emitters of level 1..14
 };
 struct Smem {
 	DevClass classes[256];
 	const uint16_t *blk[27];
 	const int8_t *hgt[27];
-	alignas(16) uint8_t cls[kClsCells];
+	const uint32_t *pln[27]; // per-chunk bit planes, or null (then the window is seeded from blocks)
+	alignas(16) uint8_t cls[kClsCells + 8];
 	alignas(16) uint8_t light[kLtCells + 8];
 	union {
 		Relight rl;
 		uint32_t masks[kPlanes][32][4]; // per plane row: visible, equal-right, equal-below, transparent pass
 	} u;
+	union {
+		struct {
+			uint64_t oc[kCls * kCls]; // x-row bits (bit = x + 1) of opaque full cubes, row = (z+1) + 34 (y+1)
+			uint64_t em[kCls * kCls]; // ... of blocks with no texture and no custom mesh
+		} pl;
+		uint2 quads[kQuadBuf]; // staged quad records
+	} aux;
 	uint32_t seg_cnt[2][kSegments + 1];
 	uint32_t seg_base[3][kSegments + 1]; // per stream and all-stream exclusive prefix
 	uint32_t warp_sum[3][kWarps];
@@ -113,7 +128,7 @@ struct Smem {
 	uint32_t misc[16];
 };
 
-__device__ __forceinline__ int cls_index(int x, int y, int z) { return ((y + 1) * kClsZ + (z + 2)) * kClsX + (x + 2); }
+__device__ __forceinline__ int cls_index(int x, int y, int z) { return ((y + 1) * kCls + (z + 1)) * kCls + (x + 1); }
 __device__ __forceinline__ int lt_index(int x, int y, int z) { return ((y + 1) * kLt + (z + 1)) * kLt + (x + 1); }
 
 // Neighbour chunk index of a cell in [-32, 64)^3 (common/include/common/Position.hpp:138-145).
@@ -195,11 +210,30 @@ struct Light4 {
 
 __device__ __forceinline__ uint32_t div_small(uint32_t v, uint32_t n) { return v / n; }
 
+// Index offsets of the same neighbours in the 34^3 class and light arrays (x + 34 z + 34^2 y).
+__host__ __device__ constexpr int cell_offset(int dx, int dy, int dz) { return dx + kCls * dz + kCls * kCls * dy; }
+#define HC_O(a, b, c) cell_offset(a, b, c)
+__constant__ int16_t c_front_off[6] = {HC_O(1, 0, 0), HC_O(-1, 0, 0), HC_O(0, 1, 0), HC_O(0, -1, 0), HC_O(0, 0, 1), HC_O(0, 0, -1)};
+__constant__ int16_t c_corner_off[6][4][3] = {
+    {{HC_O(1, 0, -1), HC_O(1, -1, -1), HC_O(1, -1, 0)}, {HC_O(1, 0, -1), HC_O(1, 1, -1), HC_O(1, 1, 0)},
+     {HC_O(1, 0, 1), HC_O(1, 1, 1), HC_O(1, 1, 0)}, {HC_O(1, 0, 1), HC_O(1, -1, 1), HC_O(1, -1, 0)}},
+    {{HC_O(-1, 0, -1), HC_O(-1, -1, -1), HC_O(-1, -1, 0)}, {HC_O(-1, 0, 1), HC_O(-1, -1, 1), HC_O(-1, -1, 0)},
+     {HC_O(-1, 0, 1), HC_O(-1, 1, 1), HC_O(-1, 1, 0)}, {HC_O(-1, 0, -1), HC_O(-1, 1, -1), HC_O(-1, 1, 0)}},
+    {{HC_O(0, 1, -1), HC_O(-1, 1, -1), HC_O(-1, 1, 0)}, {HC_O(0, 1, 1), HC_O(-1, 1, 1), HC_O(-1, 1, 0)},
+     {HC_O(0, 1, 1), HC_O(1, 1, 1), HC_O(1, 1, 0)}, {HC_O(0, 1, -1), HC_O(1, 1, -1), HC_O(1, 1, 0)}},
+    {{HC_O(0, -1, -1), HC_O(-1, -1, -1), HC_O(-1, -1, 0)}, {HC_O(0, -1, -1), HC_O(1, -1, -1), HC_O(1, -1, 0)},
+     {HC_O(0, -1, 1), HC_O(1, -1, 1), HC_O(1, -1, 0)}, {HC_O(0, -1, 1), HC_O(-1, -1, 1), HC_O(-1, -1, 0)}},
+    {{HC_O(0, -1, 1), HC_O(-1, -1, 1), HC_O(-1, 0, 1)}, {HC_O(0, -1, 1), HC_O(1, -1, 1), HC_O(1, 0, 1)},
+     {HC_O(0, 1, 1), HC_O(1, 1, 1), HC_O(1, 0, 1)}, {HC_O(0, 1, 1), HC_O(-1, 1, 1), HC_O(-1, 0, 1)}},
+    {{HC_O(0, -1, -1), HC_O(-1, -1, -1), HC_O(-1, 0, -1)}, {HC_O(0, 1, -1), HC_O(-1, 1, -1), HC_O(-1, 0, -1)},
+     {HC_O(0, 1, -1), HC_O(1, 1, -1), HC_O(1, 0, -1)}, {HC_O(0, -1, -1), HC_O(1, -1, -1), HC_O(1, 0, -1)}}};
+#undef HC_O
+
 __device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
-	const int fx = x + c_front[face][0], fy = y + c_front[face][1], fz = z + c_front[face][2];
-	const DevClass &kf = S.classes[class_at(S, fx, fy, fz)];
-	const bool dp3 = kf.flags & kFDirect;
-	const uint8_t lf = S.light[lt_index(fx, fy, fz)];
+	const int base = cls_index(x, y, z);
+	const int fi = base + c_front_off[face];
+	const bool dp3 = S.classes[S.cls[fi]].flags & kFDirect;
+	const uint8_t lf = S.light[fi];
 	Light4 r{0, 0, 0};
 #pragma unroll
 	for (int v = 0; v < 4; ++v) {
@@ -207,11 +241,11 @@ __device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
 		uint8_t l[3];
 #pragma unroll
 		for (int b = 0; b < 3; ++b) {
-			const int cx = x + c_corner[face][v][b][0], cy = y + c_corner[face][v][b][1], cz = z + c_corner[face][v][b][2];
-			const uint8_t fl = S.classes[class_at(S, cx, cy, cz)].flags;
+			const int ci = base + c_corner_off[face][v][b];
+			const uint8_t fl = S.classes[S.cls[ci]].flags;
 			ip[b] = fl & kFIndirect;
 			dp[b] = fl & kFDirect;
-			l[b] = S.light[lt_index(cx, cy, cz)];
+			l[b] = S.light[ci];
 		}
 		const int blocked = !dp[0] + !dp[1] + !dp[2] + !dp3;
 		const uint32_t ao = ((!dp[0] && !dp[2]) || (!dp[1] && !dp3)) ? 0u : (uint32_t)(3 - blocked > 0 ? 3 - blocked : 0);

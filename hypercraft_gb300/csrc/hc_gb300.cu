@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -10,6 +11,7 @@
 
 #include "../../include/hc_gb300.h"
 #include "hc_mesh.cuh"
+#include "hc_world.cuh"
 #include "hc_registry.h"
 
 namespace hc {
@@ -17,6 +19,7 @@ namespace hc {
 struct Refs27 {
 	const uint16_t *blk[27];
 	const int8_t *hgt[27];
+	const uint32_t *pln[27]; // null: seed the relight window from the blocks
 };
 
 __device__ __forceinline__ Smem &smem() {
@@ -30,9 +33,51 @@ __global__ void __launch_bounds__(kThreads, 1) k_mesh_single(Refs27 refs, DevTab
 	if (threadIdx.x < 27) {
 		S.blk[threadIdx.x] = refs.blk[threadIdx.x];
 		S.hgt[threadIdx.x] = refs.hgt[threadIdx.x];
+		S.pln[threadIdx.x] = refs.pln[threadIdx.x];
 	}
 	__syncthreads();
 	mesh_chunk_cta(S, T, A, 0);
+}
+
+// Bit planes of chunks: one thread per 32-cell row, 32 rows (one flag word) per warp.
+__device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hgt, const DevClass *cls_smem,
+                                           const uint8_t *class_of, int r, uint32_t *out) {
+	uint32_t pass, sun, t15;
+	const bool low = chunk_plane_row(blk, hgt, cls_smem, class_of, r >> 5, r & 31, pass, sun, t15);
+	out[kPlanePass * kPlaneWords + r] = pass;
+	out[kPlaneSun * kPlaneWords + r] = sun;
+	out[kPlaneT15 * kPlaneWords + r] = t15;
+	const uint32_t lows = __ballot_sync(0xffffffffu, low);
+	if ((threadIdx.x & 31) == 0)
+		out[3 * kPlaneWords + (r >> 5)] = lows;
+}
+
+// Planes of the listed pool slots (grid-stride over slot x row).
+__global__ void __launch_bounds__(256) k_planes_pool(const uint16_t *pool_blocks, const int8_t *pool_heights,
+                                                      const int32_t *slots, uint32_t n, DevTables T, uint32_t *planes) {
+	__shared__ DevClass cls[256];
+	for (int i = threadIdx.x; i < 256; i += blockDim.x)
+		cls[i] = T.classes[i];
+	__syncthreads();
+	const uint64_t total = (uint64_t)n * kPlaneWords;
+	for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x) {
+		const uint32_t i = (uint32_t)(g / kPlaneWords), r = (uint32_t)(g % kPlaneWords);
+		const size_t slot = (size_t)slots[i];
+		planes_row(pool_blocks + slot * 32768, pool_heights + slot * 1024, cls, T.class_of, (int)r,
+		           planes + slot * kPlaneStride);
+	}
+}
+
+// Planes of the 27 chunks of a single-chunk call.
+__global__ void __launch_bounds__(256) k_planes_refs(Refs27 refs, DevTables T, uint32_t *planes) {
+	__shared__ DevClass cls[256];
+	for (int i = threadIdx.x; i < 256; i += blockDim.x)
+		cls[i] = T.classes[i];
+	__syncthreads();
+	const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+	const uint32_t i = g / kPlaneWords, r = g % kPlaneWords;
+	if (i < 27)
+		planes_row(refs.blk[i], refs.hgt[i], cls, T.class_of, (int)r, planes + (size_t)i * kPlaneStride);
 }
 
 // Relight only, writing the 34^3 region the mesher reads.
@@ -41,6 +86,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_relight_single(Refs27 refs, Dev
 	if (threadIdx.x < 27) {
 		S.blk[threadIdx.x] = refs.blk[threadIdx.x];
 		S.hgt[threadIdx.x] = refs.hgt[threadIdx.x];
+		S.pln[threadIdx.x] = refs.pln[threadIdx.x];
 	}
 	for (int i = threadIdx.x; i < 256; i += kThreads)
 		S.classes[i] = T.classes[i];
@@ -54,8 +100,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_relight_single(Refs27 refs, Dev
 enum : uint32_t { kChunkBadSlot = 2 };
 
 // Points S.blk / S.hgt at the 27 neighbour slots of batch item `item`; false if a slot is invalid.
-__device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *pool_heights, uint32_t pool_cap,
-                          const int32_t *nbr, uint32_t item) {
+__device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes,
+                          uint32_t pool_cap, const int32_t *nbr, uint32_t item) {
 	__shared__ int s_bad;
 	if (threadIdx.x == 0)
 		s_bad = 0;
@@ -66,9 +112,11 @@ __device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *po
 			s_bad = 1;
 			S.blk[threadIdx.x] = pool_blocks;
 			S.hgt[threadIdx.x] = pool_heights;
+			S.pln[threadIdx.x] = nullptr;
 		} else {
 			S.blk[threadIdx.x] = pool_blocks + (size_t)slot * 32768;
 			S.hgt[threadIdx.x] = pool_heights + (size_t)slot * 1024;
+			S.pln[threadIdx.x] = pool_planes ? pool_planes + (size_t)slot * kPlaneStride : nullptr;
 		}
 	}
 	__syncthreads();
@@ -86,8 +134,8 @@ __device__ void bad_item(const Arena &A, uint32_t item, unsigned int *failed) {
 
 // Batched form: a persistent grid; each CTA takes the next chunk from a device work counter.
 __global__ void __launch_bounds__(kThreads, 1)
-    k_mesh_batch(const uint16_t *pool_blocks, const int8_t *pool_heights, uint32_t pool_cap, const int32_t *nbr, uint32_t n,
-                 unsigned int *work, unsigned int *failed, DevTables T, Arena A) {
+    k_mesh_batch(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
+                 const int32_t *nbr, uint32_t n, unsigned int *work, unsigned int *failed, DevTables T, Arena A) {
 	Smem &S = smem();
 	__shared__ uint32_t s_item;
 	for (;;) {
@@ -97,7 +145,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 		const uint32_t item = s_item;
 		if (item >= n)
 			break;
-		if (load_refs(S, pool_blocks, pool_heights, pool_cap, nbr, item)) {
+		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item)) {
 			mesh_chunk_cta(S, T, A, item);
 			if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
 				atomicAdd(failed, 1u);
@@ -110,10 +158,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 // Plain form at scale: one launch per chunk.
 __global__ void __launch_bounds__(kThreads, 1)
-    k_mesh_item(const uint16_t *pool_blocks, const int8_t *pool_heights, uint32_t pool_cap, const int32_t *nbr, uint32_t item,
-                unsigned int *failed, DevTables T, Arena A) {
+    k_mesh_item(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
+                const int32_t *nbr, uint32_t item, unsigned int *failed, DevTables T, Arena A) {
 	Smem &S = smem();
-	if (load_refs(S, pool_blocks, pool_heights, pool_cap, nbr, item)) {
+	if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item)) {
 		mesh_chunk_cta(S, T, A, item);
 		if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
 			atomicAdd(failed, 1u);
@@ -131,6 +179,7 @@ struct hc_pool {
 	uint32_t capacity = 0;
 	uint16_t *d_blocks = nullptr;
 	int8_t *d_heights = nullptr;
+	uint32_t *d_planes = nullptr; // per-slot bit planes, refreshed by every batch run for its slots
 };
 
 struct hc_batch_plan {
@@ -141,6 +190,8 @@ struct hc_batch_plan {
 	hc_batch_arena arena{};
 	int mode = HC_BATCH_PERSISTENT;
 	int grid = 0;
+	int32_t *d_slots = nullptr;            // distinct valid slots the batch reads (their planes are refreshed)
+	uint32_t n_slots = 0;
 	unsigned long long *d_state = nullptr; // quad cursor, mesh cursor, work counter, failed chunks
 	unsigned long long *h_state = nullptr; // pinned
 	cudaGraph_t graph = nullptr;
@@ -162,6 +213,7 @@ struct hc_ctx {
 	uint2 *d_verts = nullptr;
 	uint16_t *d_idx = nullptr;
 	hc_mesh_desc *d_meshes = nullptr;
+	uint32_t *d_planes = nullptr;           // bit planes of the 27 chunks of a single-chunk call
 	unsigned long long *d_cursor = nullptr; // [0] quads, [1] meshes (as unsigned int in the low word)
 	uint32_t *d_results = nullptr;
 	uint32_t *h_results = nullptr; // pinned, 8 words
@@ -269,12 +321,25 @@ hc_status upload_tables(hc_ctx *ctx) {
 
 DevTables tables(const hc_ctx *ctx) { return DevTables{ctx->d_class_of, ctx->d_classes}; }
 
-hc_status check_refs(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27]) {
+hc_status check_refs(hc_ctx *ctx, const uint16_t *const blocks[27], const int8_t *const heights[27],
+                     bool device_pointers = false) {
 	if (!blocks || !heights)
 		return fail(ctx, HC_ERR_INVALID_ARG, "null neighbour array");
-	for (int i = 0; i < 27; ++i)
+	for (int i = 0; i < 27; ++i) {
 		if (!blocks[i] || !heights[i])
 			return fail(ctx, HC_ERR_INVALID_ARG, "null chunk pointer at neighbour " + std::to_string(i));
+		if (device_pointers && ((reinterpret_cast<uintptr_t>(blocks[i]) | reinterpret_cast<uintptr_t>(heights[i])) & 15u))
+			return fail(ctx, HC_ERR_INVALID_ARG, "chunk arrays must be 16-byte aligned (neighbour " + std::to_string(i) + ")");
+	}
+	return HC_OK;
+}
+
+// Computes the bit planes of the 27 chunks into the context and points refs at them.
+hc_status planes_for_refs(hc_ctx *ctx, Refs27 &refs, cudaStream_t st) {
+	for (int i = 0; i < 27; ++i)
+		refs.pln[i] = ctx->d_planes + (size_t)i * kPlaneStride;
+	k_planes_refs<<<27 * kPlaneWords / 256, 256, 0, st>>>(refs, tables(ctx), ctx->d_planes);
+	HC_CUDA(ctx, cudaGetLastError());
 	return HC_OK;
 }
 
@@ -284,7 +349,11 @@ hc_status run_single(hc_ctx *ctx, const Refs27 &refs, uint2 *verts, uint16_t *id
 	HC_CUDA(ctx, cudaMemsetAsync(ctx->d_cursor, 0, 2 * sizeof(unsigned long long), st));
 	Arena A{verts, idx, meshes, ctx->d_cursor, reinterpret_cast<unsigned int *>(ctx->d_cursor + 1), quad_cap, mesh_cap,
 	        ctx->d_results};
-	k_mesh_single<<<1, kThreads, ctx->smem_bytes, st>>>(refs, tables(ctx), A);
+	Refs27 r = refs;
+	hc_status s = planes_for_refs(ctx, r, st);
+	if (s != HC_OK)
+		return s;
+	k_mesh_single<<<1, kThreads, ctx->smem_bytes, st>>>(r, tables(ctx), A);
 	HC_CUDA(ctx, cudaGetLastError());
 	HC_CUDA(ctx, cudaMemcpyAsync(ctx->h_results, ctx->d_results, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
 	HC_CUDA(ctx, cudaStreamSynchronize(st));
@@ -364,6 +433,7 @@ hc_status hc_ctx_create(int device, hc_ctx **out) {
 		chk(cudaMalloc(&ctx->d_verts, (size_t)HC_CHUNK_MAX_QUADS * 4 * sizeof(uint2)), "vertices");
 		chk(cudaMalloc(&ctx->d_idx, (size_t)HC_CHUNK_MAX_QUADS * 6 * sizeof(uint16_t)), "indices");
 		chk(cudaMalloc(&ctx->d_meshes, HC_CHUNK_MAX_MESHES * sizeof(hc_mesh_desc)), "meshes");
+		chk(cudaMalloc(&ctx->d_planes, 27 * (size_t)kPlaneStride * sizeof(uint32_t)), "planes");
 		chk(cudaMalloc(&ctx->d_cursor, 2 * sizeof(unsigned long long)), "cursor");
 		chk(cudaMalloc(&ctx->d_results, 8 * sizeof(uint32_t)), "results");
 		chk(cudaMallocHost(&ctx->h_results, 8 * sizeof(uint32_t)), "pinned results");
@@ -390,6 +460,7 @@ void hc_ctx_destroy(hc_ctx *ctx) {
 	cudaFree(ctx->d_verts);
 	cudaFree(ctx->d_idx);
 	cudaFree(ctx->d_meshes);
+	cudaFree(ctx->d_planes);
 	cudaFree(ctx->d_cursor);
 	cudaFree(ctx->d_results);
 	cudaFreeHost(ctx->h_results);
@@ -449,7 +520,7 @@ hc_status hc_mesh_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27], co
                                hc_chunk_mesh *out, void *stream) {
 	if (!ctx || !out)
 		return HC_ERR_INVALID_ARG;
-	hc_status s = check_refs(ctx, blocks, heights);
+	hc_status s = check_refs(ctx, blocks, heights, true);
 	if (s != HC_OK)
 		return s;
 	if (!out->meshes || !out->vertices || !out->indices)
@@ -481,7 +552,7 @@ hc_status hc_relight_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27],
                                   uint8_t *light34, void *stream) {
 	if (!ctx || !light34)
 		return HC_ERR_INVALID_ARG;
-	hc_status s = check_refs(ctx, blocks, heights);
+	hc_status s = check_refs(ctx, blocks, heights, true);
 	if (s != HC_OK)
 		return s;
 	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
@@ -491,6 +562,8 @@ hc_status hc_relight_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27],
 		refs.blk[i] = blocks[i];
 		refs.hgt[i] = heights[i];
 	}
+	if ((s = planes_for_refs(ctx, refs, st)) != HC_OK)
+		return s;
 	k_relight_single<<<1, kThreads, ctx->smem_bytes, st>>>(refs, tables(ctx), light34);
 	HC_CUDA(ctx, cudaGetLastError());
 	HC_CUDA(ctx, cudaStreamSynchronize(st));
@@ -508,6 +581,8 @@ hc_status hc_pool_create(hc_ctx *ctx, uint32_t capacity, hc_pool **out) {
 	cudaError_t e = cudaMalloc(&p->d_blocks, (size_t)capacity * 32768 * sizeof(uint16_t));
 	if (e == cudaSuccess)
 		e = cudaMalloc(&p->d_heights, (size_t)capacity * 1024);
+	if (e == cudaSuccess)
+		e = cudaMalloc(&p->d_planes, (size_t)capacity * kPlaneStride * sizeof(uint32_t));
 	if (e != cudaSuccess) {
 		hc_pool_destroy(p);
 		return fail(ctx, e == cudaErrorMemoryAllocation ? HC_ERR_OUT_OF_MEMORY : HC_ERR_CUDA,
@@ -523,6 +598,7 @@ void hc_pool_destroy(hc_pool *pool) {
 	cudaSetDevice(pool->ctx->device);
 	cudaFree(pool->d_blocks);
 	cudaFree(pool->d_heights);
+	cudaFree(pool->d_planes);
 	delete pool;
 }
 
@@ -552,6 +628,25 @@ hc_status hc_pool_upload(hc_pool *pool, uint32_t first, uint32_t count, const ui
 	return HC_OK;
 }
 
+hc_status hc_pool_download(hc_pool *pool, uint32_t first, uint32_t count, uint16_t *blocks, int8_t *heights,
+                           int dst_on_device, void *stream) {
+	if (!pool || (!blocks && !heights))
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = pool->ctx;
+	if ((uint64_t)first + count > pool->capacity)
+		return fail(ctx, HC_ERR_INVALID_ARG, "download beyond the pool capacity");
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	const cudaMemcpyKind kind = dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	if (blocks)
+		HC_CUDA(ctx, cudaMemcpyAsync(blocks, pool->d_blocks + (size_t)first * 32768,
+		                             (size_t)count * 32768 * sizeof(uint16_t), kind, st));
+	if (heights)
+		HC_CUDA(ctx, cudaMemcpyAsync(heights, pool->d_heights + (size_t)first * 1024, (size_t)count * 1024, kind, st));
+	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	return HC_OK;
+}
+
 namespace {
 
 Arena plan_arena(const hc_batch_plan *p) {
@@ -568,17 +663,25 @@ Arena plan_arena(const hc_batch_plan *p) {
 hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 	hc_ctx *ctx = p->ctx;
 	HC_CUDA(ctx, cudaMemsetAsync(p->d_state, 0, 4 * sizeof(unsigned long long), st));
+	if (p->n_slots) {
+		const uint64_t rows = (uint64_t)p->n_slots * kPlaneWords;
+		const int blocks = (int)std::min<uint64_t>((rows + 255) / 256, (uint64_t)p->grid * 8);
+		k_planes_pool<<<blocks, 256, 0, st>>>(p->pool->d_blocks, p->pool->d_heights, p->d_slots, p->n_slots, tables(ctx),
+		                                     p->pool->d_planes);
+		HC_CUDA(ctx, cudaGetLastError());
+	}
 	const Arena A = plan_arena(p);
 	unsigned int *work = reinterpret_cast<unsigned int *>(p->d_state + 2);
 	unsigned int *failed = reinterpret_cast<unsigned int *>(p->d_state + 3);
 	if (p->mode == HC_BATCH_PERSISTENT) {
-		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(p->pool->d_blocks, p->pool->d_heights, p->pool->capacity,
-		                                                          p->nbr, p->n, work, failed, tables(ctx), A);
+		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(p->pool->d_blocks, p->pool->d_heights, p->pool->d_planes,
+		                                                          p->pool->capacity, p->nbr, p->n, work, failed,
+		                                                          tables(ctx), A);
 		HC_CUDA(ctx, cudaGetLastError());
 	} else {
 		for (uint32_t i = 0; i < p->n; ++i) {
-			k_mesh_item<<<1, kThreads, ctx->smem_bytes, st>>>(p->pool->d_blocks, p->pool->d_heights, p->pool->capacity,
-			                                                  p->nbr, i, failed, tables(ctx), A);
+			k_mesh_item<<<1, kThreads, ctx->smem_bytes, st>>>(p->pool->d_blocks, p->pool->d_heights, p->pool->d_planes,
+			                                                  p->pool->capacity, p->nbr, i, failed, tables(ctx), A);
 		}
 		HC_CUDA(ctx, cudaGetLastError());
 	}
@@ -616,7 +719,22 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 		per_sm = ctas_per_sm;
 	p->grid = sms * per_sm;
 	hc_status s = HC_OK;
-	cudaError_t e = cudaMalloc(&p->d_state, 4 * sizeof(unsigned long long));
+	// distinct valid slots named by the neighbour table
+	std::vector<int32_t> table((size_t)n * 27);
+	cudaError_t e = cudaMemcpy(table.data(), neighbours, table.size() * sizeof(int32_t), cudaMemcpyDeviceToHost);
+	if (e == cudaSuccess) {
+		std::vector<uint8_t> used(pool->capacity, 0);
+		std::vector<int32_t> slots;
+		for (int32_t v : table)
+			if (v >= 0 && (uint32_t)v < pool->capacity && !used[v])
+				used[v] = 1, slots.push_back(v);
+		p->n_slots = (uint32_t)slots.size();
+		e = cudaMalloc(&p->d_slots, std::max<size_t>(1, slots.size()) * sizeof(int32_t));
+		if (e == cudaSuccess && !slots.empty())
+			e = cudaMemcpy(p->d_slots, slots.data(), slots.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+	}
+	if (e == cudaSuccess)
+		e = cudaMalloc(&p->d_state, 4 * sizeof(unsigned long long));
 	if (e == cudaSuccess)
 		e = cudaMallocHost(&p->h_state, 4 * sizeof(unsigned long long));
 	if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT) {
@@ -653,6 +771,7 @@ void hc_batch_plan_destroy(hc_batch_plan *plan) {
 		cudaGraphDestroy(plan->graph);
 	if (plan->capture_stream)
 		cudaStreamDestroy(plan->capture_stream);
+	cudaFree(plan->d_slots);
 	cudaFree(plan->d_state);
 	cudaFreeHost(plan->h_state);
 	delete plan;
@@ -711,6 +830,190 @@ hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t m
 		HC_CUDA(ctx, cudaMemcpyAsync(results, plan->arena.results, (size_t)plan->n * 5 * sizeof(uint32_t),
 		                             cudaMemcpyDeviceToHost, st));
 	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	return HC_OK;
+}
+
+} // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// Worlds: edits, height recomputation and remeshing of the chunks they touch.
+// ------------------------------------------------------------------------------------------------
+struct hc_world {
+	hc_ctx *ctx = nullptr;
+	hc_pool *pool = nullptr;
+	hc_world_desc desc{};
+	int cells = 0;
+	int32_t *d_slots = nullptr;
+	uint8_t *d_dirty = nullptr, *d_hchg = nullptr, *d_slot_mark = nullptr;
+	uint32_t *d_flood = nullptr;
+	hc_edit *d_edits = nullptr;
+	int32_t *d_list = nullptr, *d_nbr = nullptr, *d_slot_list = nullptr;
+	uint32_t *d_count = nullptr, *h_count = nullptr;
+	unsigned long long *d_state = nullptr, *h_state = nullptr;
+	int sms = 0;
+};
+
+namespace {
+
+WorldDev world_dev(const hc_world *w) {
+	return WorldDev{w->desc.nx,  w->desc.ny,  w->desc.nz,   w->desc.cx0, w->desc.cy0,      w->desc.cz0,
+	                w->d_slots,  w->d_dirty,  w->d_hchg,    w->d_flood,  w->pool->d_blocks, w->pool->d_heights};
+}
+
+} // namespace
+
+extern "C" {
+
+hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc, const int32_t *slots, hc_world **out) {
+	if (!ctx || !pool || !desc || !slots || !out || desc->nx <= 0 || desc->ny <= 0 || desc->nz <= 0 || desc->ny > 32)
+		return HC_ERR_INVALID_ARG;
+	const long long cells = (long long)desc->nx * desc->ny * desc->nz;
+	if (cells > (1ll << 21))
+		return fail(ctx, HC_ERR_INVALID_ARG, "world grid larger than 2^21 chunks");
+	for (long long i = 0; i < cells; ++i)
+		if (slots[i] >= (int32_t)pool->capacity)
+			return fail(ctx, HC_ERR_INVALID_ARG, "world slot beyond the pool capacity");
+	*out = nullptr;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	hc_world *w = new hc_world();
+	w->ctx = ctx, w->pool = pool, w->desc = *desc, w->cells = (int)cells;
+	cudaDeviceGetAttribute(&w->sms, cudaDevAttrMultiProcessorCount, ctx->device);
+	const size_t cols = (size_t)desc->nx * desc->nz * 1024;
+	cudaError_t e = cudaSuccess;
+	const auto A = [&](void **p, size_t bytes) {
+		if (e == cudaSuccess)
+			e = cudaMalloc(p, bytes > 0 ? bytes : 1);
+		if (e == cudaSuccess)
+			e = cudaMemset(*p, 0, bytes > 0 ? bytes : 1);
+	};
+	A((void **)&w->d_slots, cells * sizeof(int32_t));
+	A((void **)&w->d_dirty, cells);
+	A((void **)&w->d_hchg, cells);
+	A((void **)&w->d_flood, cols * sizeof(uint32_t));
+	A((void **)&w->d_edits, kEditBatch * sizeof(hc_edit));
+	A((void **)&w->d_list, cells * sizeof(int32_t));
+	A((void **)&w->d_nbr, cells * 27 * sizeof(int32_t));
+	A((void **)&w->d_slot_mark, pool->capacity);
+	A((void **)&w->d_slot_list, (size_t)pool->capacity * sizeof(int32_t));
+	A((void **)&w->d_count, 2 * sizeof(uint32_t));
+	A((void **)&w->d_state, 4 * sizeof(unsigned long long));
+	if (e == cudaSuccess)
+		e = cudaMallocHost(&w->h_count, 2 * sizeof(uint32_t));
+	if (e == cudaSuccess)
+		e = cudaMallocHost(&w->h_state, 4 * sizeof(unsigned long long));
+	if (e == cudaSuccess)
+		e = cudaMemcpy(w->d_slots, slots, cells * sizeof(int32_t), cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) {
+		hc_world_destroy(w);
+		return fail(ctx, e == cudaErrorMemoryAllocation ? HC_ERR_OUT_OF_MEMORY : HC_ERR_CUDA,
+		            std::string("world: ") + cudaGetErrorString(e));
+	}
+	*out = w;
+	return HC_OK;
+}
+
+void hc_world_destroy(hc_world *w) {
+	if (!w)
+		return;
+	cudaSetDevice(w->ctx->device);
+	cudaFree(w->d_slots);
+	cudaFree(w->d_dirty);
+	cudaFree(w->d_hchg);
+	cudaFree(w->d_flood);
+	cudaFree(w->d_edits);
+	cudaFree(w->d_list);
+	cudaFree(w->d_nbr);
+	cudaFree(w->d_slot_mark);
+	cudaFree(w->d_slot_list);
+	cudaFree(w->d_count);
+	cudaFree(w->d_state);
+	cudaFreeHost(w->h_count);
+	cudaFreeHost(w->h_state);
+	delete w;
+}
+
+hc_status hc_world_apply_edits(hc_world *w, const hc_edit *edits, uint32_t n, int src_on_device, void *stream) {
+	if (!w || (!edits && n))
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = w->ctx;
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	const WorldDev W = world_dev(w);
+	for (uint32_t first = 0; first < n; first += kEditBatch) {
+		const uint32_t nb = std::min<uint32_t>(kEditBatch, n - first);
+		const hc_edit *src = edits + first;
+		if (!src_on_device) {
+			HC_CUDA(ctx, cudaMemcpyAsync(w->d_edits, src, nb * sizeof(hc_edit), cudaMemcpyHostToDevice, st));
+			src = w->d_edits;
+		}
+		k_apply_edits<<<1, kEditThreads, 0, st>>>(src, nb, W);
+		HC_CUDA(ctx, cudaGetLastError());
+		if (!src_on_device)
+			HC_CUDA(ctx, cudaStreamSynchronize(st)); // d_edits is reused by the next batch
+	}
+	const uint32_t cols = (uint32_t)(w->desc.nx * w->desc.nz) * 1024u;
+	k_flood_columns<<<(cols + 255) / 256, 256, 0, st>>>(W, tables(ctx));
+	HC_CUDA(ctx, cudaGetLastError());
+	k_mark_heights<<<(w->cells + 255) / 256, 256, 0, st>>>(W);
+	HC_CUDA(ctx, cudaGetLastError());
+	return HC_OK;
+}
+
+hc_status hc_world_remesh(hc_world *w, const hc_batch_arena *arena, int32_t *cells, uint32_t cap, uint32_t *n_remeshed,
+                          uint64_t *quads, uint32_t *meshes, void *stream) {
+	if (!w || !arena || !n_remeshed || !arena->vertices || !arena->indices || !arena->meshes || !arena->results)
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = w->ctx;
+	if ((reinterpret_cast<uintptr_t>(arena->vertices) & 15u) || (reinterpret_cast<uintptr_t>(arena->indices) & 3u))
+		return fail(ctx, HC_ERR_INVALID_ARG, "vertices must be 16-byte and indices 4-byte aligned");
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	const WorldDev W = world_dev(w);
+	k_collect<<<1, kEditThreads, 0, st>>>(W, w->d_list, w->d_nbr, w->d_slot_mark, w->pool->capacity, w->d_slot_list,
+	                                      w->d_count);
+	HC_CUDA(ctx, cudaGetLastError());
+	HC_CUDA(ctx, cudaMemcpyAsync(w->h_count, w->d_count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	const uint32_t n = w->h_count[0], ns = w->h_count[1];
+	*n_remeshed = n;
+	if (quads)
+		*quads = 0;
+	if (meshes)
+		*meshes = 0;
+	if (n == 0)
+		return HC_OK;
+	const auto remark = [&](const char *msg) {
+		k_remark<<<(n + 255) / 256, 256, 0, st>>>(W, w->d_list, n);
+		cudaStreamSynchronize(st);
+		return fail(ctx, HC_ERR_CAPACITY, msg);
+	};
+	if (n > cap || !cells)
+		return remark("cells buffer too small for the chunks to remesh");
+	HC_CUDA(ctx, cudaMemsetAsync(w->d_state, 0, 4 * sizeof(unsigned long long), st));
+	k_planes_pool<<<(int)std::min<uint64_t>(((uint64_t)ns * kPlaneWords + 255) / 256, (uint64_t)w->sms * 8), 256, 0, st>>>(
+	    w->pool->d_blocks, w->pool->d_heights, w->d_slot_list, ns, tables(ctx), w->pool->d_planes);
+	HC_CUDA(ctx, cudaGetLastError());
+	const Arena A{reinterpret_cast<uint2 *>(arena->vertices),
+	              arena->indices,
+	              arena->meshes,
+	              w->d_state,
+	              reinterpret_cast<unsigned int *>(w->d_state + 1),
+	              arena->quad_capacity,
+	              arena->mesh_capacity,
+	              arena->results};
+	k_mesh_batch<<<w->sms, kThreads, ctx->smem_bytes, st>>>(
+	    w->pool->d_blocks, w->pool->d_heights, w->pool->d_planes, w->pool->capacity, w->d_nbr, n,
+	    reinterpret_cast<unsigned int *>(w->d_state + 2), reinterpret_cast<unsigned int *>(w->d_state + 3), tables(ctx), A);
+	HC_CUDA(ctx, cudaGetLastError());
+	HC_CUDA(ctx, cudaMemcpyAsync(w->h_state, w->d_state, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+	HC_CUDA(ctx, cudaMemcpyAsync(cells, w->d_list, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	if (quads)
+		*quads = w->h_state[0];
+	if (meshes)
+		*meshes = (uint32_t)(w->h_state[1] & 0xffffffffu);
+	if (w->h_state[0] > arena->quad_capacity || (w->h_state[1] & 0xffffffffu) > arena->mesh_capacity)
+		return remark("arena too small for the remeshed chunks");
 	return HC_OK;
 }
 
@@ -912,8 +1215,8 @@ extern "C" hc_status hc_mesh_batch_noalloc(const uint16_t *pool_blocks, const in
 		        quad_capacity,
 		        mesh_capacity,
 		        results};
-		k_mesh_batch<<<D.sms, kThreads, sizeof(Smem), st>>>(pool_blocks, pool_heights, pool_capacity, neighbours, n,
-		                                                     state + 4, state + 5, DevTables{D.class_of, D.classes}, A);
+		k_mesh_batch<<<D.sms, kThreads, sizeof(Smem), st>>>(pool_blocks, pool_heights, nullptr, pool_capacity, neighbours,
+		                                                     n, state + 4, state + 5, DevTables{D.class_of, D.classes}, A);
 		e = cudaGetLastError();
 	}
 	uint32_t host_state[kNoAllocStateWords];

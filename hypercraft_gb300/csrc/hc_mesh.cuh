@@ -13,8 +13,8 @@
 // Parallel form. A plane's cells are keyed by (texture, Light4); the greedy merge only ever
 // compares a cell with its right and lower neighbour (equality is transitive), so each plane is
 // reduced to four 32x32 bit masks: visible, equal-to-right, equal-to-below and transparent-pass.
-// A warp builds them row by row with ballots; one thread then runs the exact sequential greedy
-// scan on the masks with word operations. Counts per (stream, segment) are prefix-summed in
+// Warps build them with ballots and then run the exact sequential greedy scan on the masks with
+// word operations, one warp per plane. Counts per (stream, segment) are prefix-summed in
 // output order, which gives every quad its final stream index k before anything is written, so
 // all quads are written in parallel straight to their reference positions.
 #pragma once
@@ -58,28 +58,55 @@ __device__ __forceinline__ void put_quad(Smem &S, const Emit &E, int st, uint32_
 
 // ------------------------------------------------------------------------------------- staging
 
-__device__ void stage_classes(Smem &S, const DevTables &T) {
+// Stages the block classes of [-1, 32]^3, one warp per (y, z) row with lanes over x (four rows in
+// flight), and builds the x-row bit planes of opaque full cubes and of blank blocks. Returns true
+// when the chunk can produce no quad: every inner block has no texture and no custom mesh, or every
+// inner block and every block of the six adjacent layers is an opaque full cube.
+__device__ bool stage_classes(Smem &S, const DevTables &T) {
 	for (int i = threadIdx.x; i < 256; i += kThreads)
 		S.classes[i] = T.classes[i];
-	for (int i = threadIdx.x; i < kClsCells; i += kThreads) {
-		const int x = i % kClsX - 2, z = (i / kClsX) % kClsZ - 2, y = i / (kClsX * kClsZ) - 1;
-		S.cls[i] = __ldg(T.class_of + raw_at(S, x, y, z));
-	}
-}
-
-// True when the chunk can produce no quad: every inner block has no texture and no custom mesh,
-// or every inner block and every block of the six adjacent layers is an opaque full cube.
-__device__ bool chunk_is_blank(Smem &S) {
+	__syncthreads();
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	constexpr int kRows = kCls * kCls, kBatch = 4; // 1156 rows
+	static_assert(kRows % kBatch == 0, "row batches");
 	bool content = false, open = false;
-	for (int i = threadIdx.x; i < kClsCells; i += kThreads) {
-		const int x = i % kClsX - 2, z = (i / kClsX) % kClsZ - 2, y = i / (kClsX * kClsZ) - 1;
-		const int out = (x < 0 || x >= kChunk) + (y < 0 || y >= kChunk) + (z < 0 || z >= kChunk);
-		const uint8_t f = S.classes[S.cls[i]].flags;
-		if (out == 0) {
-			content |= !(f & kFEmpty);
-			open |= !(f & kFOpaqueCube);
-		} else if (out == 1 && x >= -1 && x <= kChunk && z >= -1 && z <= kChunk) {
-			open |= !(f & kFOpaqueCube);
+	for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
+		uint16_t raw[kBatch], rawe[kBatch];
+#pragma unroll
+		for (int j = 0; j < kBatch; ++j) {
+			const int y = (row0 + j) / kCls - 1, z = (row0 + j) % kCls - 1;
+			raw[j] = raw_at(S, lane, y, z);
+			rawe[j] = lane < 2 ? raw_at(S, lane ? kChunk : -1, y, z) : (uint16_t)0;
+		}
+		uint8_t c[kBatch], ce[kBatch];
+#pragma unroll
+		for (int j = 0; j < kBatch; ++j) {
+			c[j] = __ldg(T.class_of + raw[j]);
+			ce[j] = __ldg(T.class_of + rawe[j]);
+		}
+#pragma unroll
+		for (int j = 0; j < kBatch; ++j) {
+			const int row = row0 + j, y = row / kCls - 1, z = row % kCls - 1;
+			uint8_t *dst = S.cls + row * kCls;
+			dst[lane + 1] = c[j];
+			if (lane < 2)
+				dst[lane ? kCls - 1 : 0] = ce[j];
+			const uint8_t f = S.classes[c[j]].flags, fe = S.classes[ce[j]].flags;
+			const uint32_t oc = __ballot_sync(0xffffffffu, f & kFOpaqueCube);
+			const uint32_t em = __ballot_sync(0xffffffffu, f & kFEmpty);
+			const uint32_t oce = __ballot_sync(0xffffffffu, lane < 2 && (fe & kFOpaqueCube));
+			const uint32_t eme = __ballot_sync(0xffffffffu, lane < 2 && (fe & kFEmpty));
+			if (lane == 0) {
+				S.aux.pl.oc[row] = (uint64_t)(oce & 1u) | ((uint64_t)oc << 1) | ((uint64_t)((oce >> 1) & 1u) << 33);
+				S.aux.pl.em[row] = (uint64_t)(eme & 1u) | ((uint64_t)em << 1) | ((uint64_t)((eme >> 1) & 1u) << 33);
+			}
+			const bool yin = y >= 0 && y < kChunk, zin = z >= 0 && z < kChunk;
+			if (yin && zin) {
+				content |= !(f & kFEmpty);
+				open |= !(f & kFOpaqueCube) || (lane < 2 && !(fe & kFOpaqueCube));
+			} else if (yin || zin) { // a face-adjacent layer row (x in [0, 32))
+				open |= !(f & kFOpaqueCube);
+			}
 		}
 	}
 	content = __syncthreads_or(content);
@@ -109,10 +136,10 @@ __device__ uint32_t custom_faces(const Smem &S, int x, int y, int z, hc_mesh_fac
 	return 0;
 }
 
-// Stream counts of the custom faces of inner blocks [first, first + 64).
+// Stream counts of the custom faces of inner blocks [first, first + kBlocksPerThread).
 __device__ void custom_count(const Smem &S, int first, uint32_t &co, uint32_t &ct) {
 	co = ct = 0;
-	for (int i = first; i < first + 64; ++i) {
+	for (int i = first; i < first + kBlocksPerThread; ++i) {
 		const int x = i & 31, z = (i >> 5) & 31, y = i >> 10;
 		const DevClass &k = S.classes[class_at(S, x, y, z)];
 		const uint32_t kind = k.mesh_meta & 3u;
@@ -139,7 +166,7 @@ __device__ __forceinline__ uint32_t tri(uint32_t l0, uint32_t l1, uint32_t l2, u
 }
 
 __device__ void custom_emit(Smem &S, const Emit &E, int first, uint32_t ko, uint32_t kt, uint32_t g) {
-	for (int i = first; i < first + 64; ++i) {
+	for (int i = first; i < first + kBlocksPerThread; ++i) {
 		const int x = i & 31, z = (i >> 5) & 31, y = i >> 10;
 		const DevClass &kc = S.classes[class_at(S, x, y, z)];
 		if ((kc.mesh_meta & 3u) == HC_MESH_NONE)
@@ -210,33 +237,99 @@ __device__ void custom_emit(Smem &S, const Emit &E, int first, uint32_t ko, uint
 
 __device__ __forceinline__ int plane_id(int axis, int slice, int inv) { return axis * 66 + slice * 2 + inv; }
 
-// Pass 1: visible and transparent-pass masks of both planes of every slice (no light needed).
-// Returns true if any face of the chunk is visible.
-__device__ bool plane_visibility(Smem &S) {
+// Pass 1 (before the relight): visibility of both face planes of every slice from the opaque-cube
+// and blank planes. Between an opaque cube and a blank block only the cube's face shows; two cubes
+// or two blanks show nothing (BlockTexture::Show); any pair involving another block ("complex":
+// transparent, liquid, custom mesh) is left to pass 1b. Writes visible bits to masks[.][u][0],
+// complex candidates to [.][u][1], zero transparent-pass bits to [.][u][3]. Lane = plane row.
+__device__ void plane_visibility(Smem &S) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	bool any = false;
-	for (int sl = warp; sl < kSlices; sl += kWarps) {
-		const int a = sl / 33, s = sl - a * 33;
-		uint32_t(*mA)[4] = S.u.masks[plane_id(a, s, 0)];
-		uint32_t(*mB)[4] = S.u.masks[plane_id(a, s, 1)];
-		for (int u = 0; u < 32; ++u) {
+	constexpr uint64_t k34 = (1ull << 34) - 1ull;
+	// y and z slices: rows straight from the x-row planes (bit x + 1 -> plane bit x)
+	for (int sl = warp; sl < 66; sl += kWarps) {
+		const int a = 1 + sl / 33, s = sl % 33, u = lane;
+		// cells n (slice coordinate s - 1) and p (slice coordinate s) of plane row u
+		const int rn = a == 1 ? (u + 1) + kCls * s : s + kCls * (u + 1);
+		const int rp = a == 1 ? (u + 1) + kCls * (s + 1) : (s + 1) + kCls * (u + 1);
+		const uint64_t ocn = S.aux.pl.oc[rn], emn = S.aux.pl.em[rn], ocp = S.aux.pl.oc[rp], emp = S.aux.pl.em[rp];
+		const uint32_t cx = (uint32_t)((((~(ocn | emn)) | (~(ocp | emp))) & k34) >> 1);
+		const uint32_t va = s != 0 ? (uint32_t)((ocn & emp) >> 1) : 0u;
+		const uint32_t vb = s != 32 ? (uint32_t)((ocp & emn) >> 1) : 0u;
+		uint32_t *mA = S.u.masks[plane_id(a, s, 0)][u];
+		uint32_t *mB = S.u.masks[plane_id(a, s, 1)][u];
+		mA[0] = va, mA[1] = s != 0 ? cx : 0u, mA[3] = 0;
+		mB[0] = vb, mB[1] = s != 32 ? cx : 0u, mB[3] = 0;
+	}
+	// x slices: per row y, lane = z holds the x-row words; faces of every slice at once, then a
+	// ballot per slice transposes them into plane rows over z
+	for (int y = warp; y < kChunk; y += kWarps) {
+		const int r = (lane + 1) + kCls * (y + 1);
+		const uint64_t oc = S.aux.pl.oc[r], em = S.aux.pl.em[r];
+		const uint64_t fa = oc & (em >> 1), fb = (oc >> 1) & em; // bit s: face at slice s
+		const uint64_t c = ~(oc | em) & k34, cxp = c | (c >> 1);
+		for (int s = 0; s <= kChunk; ++s) {
+			const uint32_t va = __ballot_sync(0xffffffffu, (fa >> s) & 1u);
+			const uint32_t vb = __ballot_sync(0xffffffffu, (fb >> s) & 1u);
+			const uint32_t cx = __ballot_sync(0xffffffffu, (cxp >> s) & 1u);
+			if (lane == 0) {
+				uint32_t *mA = S.u.masks[plane_id(0, s, 0)][y];
+				uint32_t *mB = S.u.masks[plane_id(0, s, 1)][y];
+				mA[0] = s != 0 ? va : 0u, mA[1] = s != 0 ? cx : 0u, mA[3] = 0;
+				mB[0] = s != 32 ? vb : 0u, mB[1] = s != 32 ? cx : 0u, mB[3] = 0;
+			}
+		}
+	}
+}
+
+// Pass 1b: exact Show for the complex candidates of every plane row (texture lookups, dynamic
+// liquid textures), and transparent-pass bits of the faces it shows. Lane = plane row.
+__device__ void plane_complex(Smem &S) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for (int p = warp; p < kPlanes; p += kWarps) {
+		uint32_t *m = S.u.masks[p][lane];
+		uint32_t cx = m[1];
+		if (!__any_sync(0xffffffffu, cx != 0))
+			continue;
+		const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
+		uint32_t vis = m[0], tp = 0;
+		while (cx) {
+			const int v = __ffs(cx) - 1;
+			cx &= cx - 1;
 			int x, y, z;
-			to_xyz(a, s, u, lane, x, y, z);
+			to_xyz(a, s, lane, v, x, y, z);
 			int nx = x, ny = y, nz = z;
 			(a == 0 ? nx : (a == 1 ? ny : nz)) -= 1;
 			const uint16_t ta = get_tex(S, nx, ny, nz, 2 * a), tb = get_tex(S, x, y, z, 2 * a + 1);
-			const bool va = s != 0 && show(ta, tb), vb = s != 32 && show(tb, ta);
-			const uint32_t NA = __ballot_sync(0xffffffffu, va), NB = __ballot_sync(0xffffffffu, vb);
-			const uint32_t TA = __ballot_sync(0xffffffffu, va && tex_transpass(ta));
-			const uint32_t TB = __ballot_sync(0xffffffffu, vb && tex_transpass(tb));
-			if (lane == 0) {
-				mA[u][0] = NA, mA[u][1] = 0, mA[u][2] = 0, mA[u][3] = TA;
-				mB[u][0] = NB, mB[u][1] = 0, mB[u][2] = 0, mB[u][3] = TB;
+			const uint16_t mine = inv ? tb : ta, other = inv ? ta : tb;
+			if (show(mine, other)) {
+				vis |= 1u << v;
+				if (tex_transpass(mine))
+					tp |= 1u << v;
+			} else {
+				vis &= ~(1u << v);
 			}
-			any |= (NA | NB) != 0;
+		}
+		m[0] = vis;
+		m[3] = tp;
+	}
+}
+
+// Position of the n-th (0-based) set bit of mask (n < popc(mask)), by halving the search window.
+__device__ __forceinline__ int nth_set_bit(uint32_t mask, uint32_t n) {
+	int pos = 0;
+#pragma unroll
+	for (int w = 16; w > 0; w >>= 1) {
+		const uint32_t low = mask & ((1u << w) - 1u);
+		const uint32_t c = __popc(low);
+		if (n >= c) {
+			n -= c;
+			mask >>= w;
+			pos += w;
+		} else {
+			mask = low;
 		}
 	}
-	return __syncthreads_or(any);
+	return pos;
 }
 
 struct Key {
@@ -265,116 +358,237 @@ __device__ __forceinline__ Key face_key(const Smem &S, int a, int s, int inv, in
 	return Key{(uint32_t)t | (l.ao << 16), l.sun, l.torch};
 }
 
-// Pass 2 (after relight): equal-to-right and equal-to-below masks of both planes of every slice.
+// Pass 2 (after the relight): equal-to-right and equal-to-below masks of every plane. The visible
+// faces of a plane are taken in batches of whole rows (at most 32 faces), one face per lane, so
+// the light keys are computed by full warps; a face's right neighbour is the next lane and its
+// upper neighbour sits in this batch or in the previous one.
 __device__ void plane_keys(Smem &S) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int sl = warp; sl < kSlices; sl += kWarps) {
-		const int a = sl / 33, s = sl - a * 33;
+	for (int p = warp; p < kPlanes; p += kWarps) {
+		uint32_t *mrow = S.u.masks[p][lane];
+		const uint32_t N = mrow[0];
+		mrow[1] = 0;
+		mrow[2] = 0;
+		const uint32_t cnt = __popc(N);
+		uint32_t incl = cnt;
 #pragma unroll
-		for (int inv = 0; inv < 2; ++inv) {
-			uint32_t(*m)[4] = S.u.masks[plane_id(a, s, inv)];
-			Key prev{0, 0, 0};
-			bool prev_vis = false;
-			for (int u = 0; u < 32; ++u) {
-				const uint32_t N = m[u][0];
-				if (!N) { // nothing visible: no run continues here and nothing matches the row above
-					if (lane == 0) {
-						m[u][1] = 0;
-						if (u > 0)
-							m[u - 1][2] = 0;
-					}
-					prev_vis = false;
-					continue;
-				}
-				const bool vis = (N >> lane) & 1u;
-				Key k{0, 0, 0};
-				if (vis)
-					k = face_key(S, a, s, inv, u, lane, nullptr, nullptr);
-				const Key right = shfl_down_key(k);
-				const bool rv = lane < 31 && ((N >> (lane + 1)) & 1u);
-				const uint32_t E = __ballot_sync(0xffffffffu, vis && rv && key_eq(k, right));
-				const uint32_t D = __ballot_sync(0xffffffffu, vis && prev_vis && key_eq(k, prev));
-				if (lane == 0) {
-					m[u][1] = E;
-					if (u > 0)
-						m[u - 1][2] = D; // bit v: rows u-1 and u hold the same face key at column v
-				}
-				prev = k;
-				prev_vis = vis;
-			}
-			if (lane == 0)
-				m[31][2] = 0;
+		for (int d = 1; d < 32; d <<= 1) {
+			const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+			if (lane >= d)
+				incl += o;
 		}
+		const uint32_t start = incl - cnt;
+		const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+		__syncwarp();
+		if (total == 0)
+			continue;
+		const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
+		Key prev{0, 0, 0};
+		uint32_t prev_b = 0, b = 0;
+		int ub = 0;
+		while (b < total) {
+			// rows [ub, ue) whose faces fit in 32 lanes from index b
+			const uint32_t over = __ballot_sync(0xffffffffu, lane >= ub && incl > b + 32);
+			const int ue = over ? __ffs(over) - 1 : 32;
+			const uint32_t be = __shfl_sync(0xffffffffu, start, ue & 31);
+			const uint32_t bend = ue < 32 ? be : total;
+			// this lane's face: compacted index f = b + lane
+			const uint32_t f = b + lane;
+			const bool has = f < bend;
+			int u = 0;
+			uint32_t k = 0;
+			for (int r = ub; r < ue; ++r) {
+				const uint32_t rs = __shfl_sync(0xffffffffu, start, r), rc = __shfl_sync(0xffffffffu, cnt, r);
+				if (f >= rs && f < rs + rc)
+					u = r, k = f - rs;
+			}
+			const uint32_t Nu = __shfl_sync(0xffffffffu, N, u);
+			const int v = has ? nth_set_bit(Nu, k) : 0;
+			Key key{0, 0, 0};
+			if (has)
+				key = face_key(S, a, s, inv, u, v, nullptr, nullptr);
+			// right neighbour: next lane when (u, v + 1) is visible
+			const Key right = shfl_down_key(key);
+			const bool rv = has && v < 31 && ((Nu >> (v + 1)) & 1u);
+			if (rv && key_eq(key, right))
+				atomicOr(&S.u.masks[p][u][1], 1u << v);
+			// upper neighbour (u - 1, v)
+			const uint32_t Nup = __shfl_sync(0xffffffffu, N, (u + 31) & 31);
+			const uint32_t sup = __shfl_sync(0xffffffffu, start, (u + 31) & 31);
+			const bool uv = has && u > 0 && ((Nup >> v) & 1u);
+			const uint32_t fi = sup + __popc(Nup & ((1u << v) - 1u));
+			const int src_cur = (int)(fi - b) & 31, src_prev = (int)(fi - prev_b) & 31;
+			const Key kc{__shfl_sync(0xffffffffu, key.tex_ao, src_cur), __shfl_sync(0xffffffffu, key.sun, src_cur),
+			             __shfl_sync(0xffffffffu, key.torch, src_cur)};
+			const Key kp{__shfl_sync(0xffffffffu, prev.tex_ao, src_prev), __shfl_sync(0xffffffffu, prev.sun, src_prev),
+			             __shfl_sync(0xffffffffu, prev.torch, src_prev)};
+			if (uv && key_eq(key, fi >= b ? kc : kp))
+				atomicOr(&S.u.masks[p][u - 1][2], 1u << v);
+			prev = key;
+			prev_b = b;
+			b = bend;
+			ub = ue;
+		}
+		__syncwarp();
 	}
 }
 
-// Exact greedy scan of one plane from its masks (BlockMeshAlgo.hpp:345-477). on_quad(u, v, w, h, st)
-// is called in the reference's order: row-major by the quad's first cell.
-template <typename F> __device__ __forceinline__ void merge_plane(const uint32_t (*m)[4], F &&on_quad) {
-	uint32_t consumed[32];
-#pragma unroll
-	for (int i = 0; i < 32; ++i)
-		consumed[i] = 0;
-	for (int u = 0; u < 32; ++u) {
-		const uint32_t live = m[u][0] & ~consumed[u];
+// Exact greedy scan of one plane from its masks (BlockMeshAlgo.hpp:345-477), one warp per plane.
+// Lane r holds row r's masks and consumed bits. For each row u (in order) the quads starting in
+// row u are its runs: maximal stretches of live cells whose right neighbours are equal (width
+// first); every run then grows down over whole rows while each of its cells equals the one above
+// (height), the runs of one row extending in lockstep and marking the cells they cover consumed.
+// on_row(u, starts, tmask, is_start, w, h) is called by the whole warp for every row with quads;
+// the quad of lane v (is_start) is (u, v, w, h) and its stream is bit v of tmask.
+template <typename F> __device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], F &&on_row) {
+	const int lane = threadIdx.x & 31;
+	const uint32_t rN = m[lane][0], rE = m[lane][1], rD = m[lane][2], rT = m[lane][3];
+	uint32_t consumed = 0; // of row `lane`
+	uint32_t rows = __ballot_sync(0xffffffffu, rN != 0);
+	while (rows) {
+		const int u = __ffs(rows) - 1;
+		rows &= rows - 1;
+		const uint32_t live = __shfl_sync(0xffffffffu, rN, u) & ~__shfl_sync(0xffffffffu, consumed, u);
 		if (!live)
 			continue;
-		const uint32_t cont = live & (live << 1) & (m[u][1] << 1); // bit v continues the run of v-1
-		uint32_t starts = live & ~cont;
-		const uint32_t tp = m[u][3];
-		while (starts) {
-			const int v = __ffs(starts) - 1;
-			starts &= starts - 1;
-			const uint32_t after = v == 31 ? 0u : (cont >> (v + 1));
-			const int w = __ffs(~after);
-			const uint32_t run = w == 32 ? 0xffffffffu : (((1u << w) - 1u) << v);
-			int h = 1;
-			while (u + h < 32 && (m[u + h - 1][2] & run) == run) {
-				consumed[u + h] |= run;
-				++h;
+		const uint32_t Eu = __shfl_sync(0xffffffffu, rE, u), Tu = __shfl_sync(0xffffffffu, rT, u);
+		const uint32_t cont = live & (live << 1) & (Eu << 1); // bit v continues the run of v-1
+		const uint32_t starts = live & ~cont;
+		const bool is_start = (starts >> lane) & 1u;
+		const uint32_t after = lane == 31 ? 0u : (cont >> (lane + 1));
+		const int w = __ffs(~after);
+		const uint32_t run = is_start ? (w == 32 ? 0xffffffffu : (((1u << w) - 1u) << lane)) : 0u;
+		int h = 1;
+		bool going = is_start;
+		for (int k = 1; u + k < 32; ++k) {
+			if (!__any_sync(0xffffffffu, going))
+				break;
+			const uint32_t below = __shfl_sync(0xffffffffu, rD, u + k - 1);
+			going = going && (below & run) == run;
+			const uint32_t grown = __reduce_or_sync(0xffffffffu, going ? run : 0u);
+			if (lane == u + k)
+				consumed |= grown;
+			if (going)
+				h = k + 1;
+		}
+		on_row(u, starts, Tu, is_start, w, h);
+	}
+}
+
+// Quad record: plane, row, column, width-1, height-1, stream; then the quad's index among the
+// plane's quads (all streams) and among the plane's quads of its stream.
+__device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, int st, uint32_t li, uint32_t lk) {
+	return make_uint2((uint32_t)p | ((uint32_t)u << 8) | ((uint32_t)v << 13) | ((uint32_t)(w - 1) << 18) |
+	                      ((uint32_t)(h - 1) << 23) | ((uint32_t)st << 28),
+	                  li | (lk << 16));
+}
+
+// Counts the quads of every plane (warp per plane) and keeps their records in shared memory while
+// they fit; misc[4] = records kept, misc[5] = 1 if some did not fit.
+__device__ void planes_count(Smem &S) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t lt = (1u << lane) - 1u;
+	for (int p = warp; p < kPlanes; p += kWarps) {
+		uint32_t n_all = 0, n_st[2] = {0, 0};
+		warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
+			const uint32_t cnt = __popc(starts);
+			uint32_t base = 0;
+			if (lane == 0)
+				base = atomicAdd(&S.misc[4], cnt);
+			base = __shfl_sync(0xffffffffu, base, 0);
+			if (is_start) {
+				const int st = (int)((tmask >> lane) & 1u);
+				const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
+				const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
+				const uint32_t slot = base + __popc(starts & lt);
+				if (slot < (uint32_t)kQuadBuf)
+					S.aux.quads[slot] = quad_record(p, u, lane, w, h, st, li, lk);
+				else
+					S.misc[5] = 1;
 			}
-			on_quad(u, v, w, h, (int)((tp >> v) & 1u));
+			n_all += cnt;
+			n_st[1] += __popc(starts & tmask);
+			n_st[0] += __popc(starts & ~tmask);
+		});
+		if (lane == 0) {
+			S.seg_cnt[0][1 + p] = n_st[0];
+			S.seg_cnt[1][1 + p] = n_st[1];
 		}
 	}
 }
 
-__device__ void plane_count(Smem &S, int p) {
-	uint32_t c[2] = {0, 0};
-	merge_plane(S.u.masks[p], [&](int, int, int, int, int st) { ++c[st]; });
-	S.seg_cnt[0][1 + p] = c[0];
-	S.seg_cnt[1][1 + p] = c[1];
-}
-
-__device__ void plane_emit(Smem &S, const Emit &E, int p) {
+// Writes quad (u, v, w, h) of plane p: stream st, stream index k, all-stream index g.
+__device__ void emit_plane_quad(Smem &S, const Emit &E, int p, int u, int v, int w, int h, int st, uint32_t k, uint32_t g) {
 	const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
 	const bool uv_cycle = a != 2; // (U + 1) % 3 == V for the YZX swizzle (BlockMeshAlgo.hpp:384)
-	uint32_t k[2] = {S.seg_base[0][1 + p], S.seg_base[1][1 + p]};
-	uint32_t g = S.seg_base[2][1 + p];
-	merge_plane(S.u.masks[p], [&](int u, int v, int w, int h, int st) {
-		uint16_t t;
-		Light4 l;
-		face_key(S, a, s, inv, u, v, &t, &l);
-		int o[3], hv[3], wv[3];
-		to_xyz(a, s, u, v, o[0], o[1], o[2]);
-		to_xyz(a, 0, h, 0, hv[0], hv[1], hv[2]);
-		to_xyz(a, 0, 0, w, wv[0], wv[1], wv[2]);
-		const bool hfirst = (inv != 0) != uv_cycle;
-		const int *du = hfirst ? hv : wv, *dv = hfirst ? wv : hv;
-		const uint32_t face = (uint32_t)(2 * a + inv);
-		uint2 vt[4];
-		const int cx[4] = {o[0], o[0] + du[0], o[0] + du[0] + dv[0], o[0] + dv[0]};
-		const int cy[4] = {o[1], o[1] + du[1], o[1] + du[1] + dv[1], o[1] + dv[1]};
-		const int cz[4] = {o[2], o[2] + du[2], o[2] + du[2] + dv[2], o[2] + dv[2]};
+	uint16_t t;
+	Light4 l;
+	face_key(S, a, s, inv, u, v, &t, &l);
+	int o[3], hv[3], wv[3];
+	to_xyz(a, s, u, v, o[0], o[1], o[2]);
+	to_xyz(a, 0, h, 0, hv[0], hv[1], hv[2]);
+	to_xyz(a, 0, 0, w, wv[0], wv[1], wv[2]);
+	const bool hfirst = (inv != 0) != uv_cycle;
+	const int *du = hfirst ? hv : wv, *dv = hfirst ? wv : hv;
+	const uint32_t face = (uint32_t)(2 * a + inv);
+	uint2 vt[4];
+	const int cx[4] = {o[0], o[0] + du[0], o[0] + du[0] + dv[0], o[0] + dv[0]};
+	const int cy[4] = {o[1], o[1] + du[1], o[1] + du[1] + dv[1], o[1] + dv[1]};
+	const int cz[4] = {o[2], o[2] + du[2], o[2] + du[2] + dv[2], o[2] + dv[2]};
 #pragma unroll
-		for (int c = 0; c < 4; ++c)
-			vt[c] = pack_vertex((uint32_t)cx[c] << 4, (uint32_t)cy[c] << 4, (uint32_t)cz[c] << 4, (uint32_t)a, face,
-			                    ao_get(l.ao, c), l4_get(l.sun, c), l4_get(l.torch, c), t);
-		const uint32_t mn[3] = {(uint32_t)cx[0] << 4, (uint32_t)cy[0] << 4, (uint32_t)cz[0] << 4};
-		const uint32_t mx[3] = {(uint32_t)cx[2] << 4, (uint32_t)cy[2] << 4, (uint32_t)cz[2] << 4};
-		put_quad(S, E, st, k[st], g, vt, flip_of(l), mn, mx);
-		++k[st];
-		++g;
-	});
+	for (int c = 0; c < 4; ++c)
+		vt[c] = pack_vertex((uint32_t)cx[c] << 4, (uint32_t)cy[c] << 4, (uint32_t)cz[c] << 4, (uint32_t)a, face,
+		                    ao_get(l.ao, c), l4_get(l.sun, c), l4_get(l.torch, c), t);
+	const uint32_t mn[3] = {(uint32_t)cx[0] << 4, (uint32_t)cy[0] << 4, (uint32_t)cz[0] << 4};
+	const uint32_t mx[3] = {(uint32_t)cx[2] << 4, (uint32_t)cy[2] << 4, (uint32_t)cz[2] << 4};
+	put_quad(S, E, st, k, g, vt, flip_of(l), mn, mx);
+}
+
+__device__ __forceinline__ void emit_record(Smem &S, const Emit &E, uint2 r) {
+	const int p = (int)(r.x & 255u), st = (int)((r.x >> 28) & 1u);
+	const uint32_t li = r.y & 0xffffu, lk = r.y >> 16;
+	emit_plane_quad(S, E, p, (int)((r.x >> 8) & 31u), (int)((r.x >> 13) & 31u), (int)((r.x >> 18) & 31u) + 1,
+	                (int)((r.x >> 23) & 31u) + 1, st, S.seg_base[st][1 + p] + lk, S.seg_base[2][1 + p] + li);
+}
+
+// Emits the plane quads. Normally planes_count kept all their records; otherwise the quads are
+// taken in windows of kQuadBuf (in output order), the planes overlapping a window re-run their
+// merge to stage that window's records, and the CTA writes them.
+__device__ void planes_emit(Smem &S, const Emit &E, uint32_t custom_all, uint32_t plane_quads) {
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	if (!S.misc[5]) {
+		for (uint32_t j = tid; j < S.misc[4]; j += kThreads)
+			emit_record(S, E, S.aux.quads[j]);
+		return;
+	}
+	const uint32_t lt = (1u << lane) - 1u;
+	for (uint32_t w0 = 0; w0 < plane_quads; w0 += kQuadBuf) {
+		for (int p = warp; p < kPlanes; p += kWarps) {
+			const uint32_t pb = S.seg_base[2][1 + p] - custom_all;
+			const uint32_t pc = S.seg_cnt[0][1 + p] + S.seg_cnt[1][1 + p];
+			if (!pc || pb >= w0 + kQuadBuf || pb + pc <= w0)
+				continue;
+			uint32_t n_all = 0, n_st[2] = {0, 0};
+			warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
+				if (is_start) {
+					const int st = (int)((tmask >> lane) & 1u);
+					const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
+					const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
+					const uint32_t i = pb + li;
+					if (i >= w0 && i < w0 + kQuadBuf)
+						S.aux.quads[i - w0] = quad_record(p, u, lane, w, h, st, li, lk);
+				}
+				n_all += __popc(starts);
+				n_st[1] += __popc(starts & tmask);
+				n_st[0] += __popc(starts & ~tmask);
+			});
+		}
+		__syncthreads();
+		const uint32_t n = min((uint32_t)kQuadBuf, plane_quads - w0);
+		for (uint32_t j = tid; j < n; j += kThreads)
+			emit_record(S, E, S.aux.quads[j]);
+		__syncthreads();
+	}
 }
 
 // --------------------------------------------------------------------------------------- scans
@@ -465,35 +679,37 @@ struct Arena {
 
 enum : uint32_t { kChunkOk = 0, kChunkCapacity = 1 };
 
-// Relights and meshes one chunk whose 27 neighbour pointers are already in S.blk / S.hgt.
+// Relights and meshes one chunk whose 27 neighbour pointers are already in S.blk / S.hgt / S.pln.
 __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint32_t pos) {
 	const int tid = threadIdx.x;
-	stage_classes(S, T);
 	for (int i = tid; i < 2 * kMaxMeshesPerStream; i += kThreads) {
 		uint32_t *bb = S.aabb[i / kMaxMeshesPerStream][i % kMaxMeshesPerStream];
 		bb[0] = bb[1] = bb[2] = 0xffffffffu;
 		bb[3] = bb[4] = bb[5] = 0u;
 	}
-	__syncthreads();
+	const bool blank = stage_classes(S, T);
 
 	uint32_t qo = 0, qt = 0;
 	uint32_t eo = 0, et = 0;
-	if (!chunk_is_blank(S)) {
+	if (!blank) {
 		uint32_t co, ct, to, tt;
-		custom_count(S, tid * 64, co, ct);
+		custom_count(S, tid * kBlocksPerThread, co, ct);
 		block_scan2(S, co, ct, eo, et, to, tt);
 		relight_window(S, T); // the relight scratch shares memory with the plane masks
 		__syncthreads();
 		plane_visibility(S);
 		__syncthreads();
+		plane_complex(S);
+		__syncthreads();
 		plane_keys(S);
 		if (tid == 0) {
 			S.seg_cnt[0][0] = to;
 			S.seg_cnt[1][0] = tt;
+			S.misc[4] = 0;
+			S.misc[5] = 0;
 		}
 		__syncthreads();
-		if (tid < kPlanes)
-			plane_count(S, tid);
+		planes_count(S);
 		__syncthreads();
 		segment_scan(S);
 		__syncthreads();
@@ -522,10 +738,9 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		return;
 
 	const Emit E{A.verts, A.idx, q0, qo};
-	custom_emit(S, E, tid * 64, eo, et, eo + et);
-	if (tid < kPlanes)
-		plane_emit(S, E, tid);
-	__syncthreads();
+	custom_emit(S, E, tid * kBlocksPerThread, eo, et, eo + et);
+	const uint32_t custom_all = S.seg_base[2][1];
+	planes_emit(S, E, custom_all, q - custom_all);
 
 	// Mesh descriptors: closed meshes in closing order, then the open opaque and transparent ones.
 	if (tid == 0) {

@@ -1,0 +1,105 @@
+"""Block edits on a resident world, then relight + remesh of the chunks they touch.
+
+Python side of include/hc_gb300.h's hc_world_* entry points, which replace the reference's edit task
+chain (client/src/ChunkSetBlockTask.cpp:37-131 -> ChunkFloodSunlightTask.cpp:33-66 ->
+ChunkSetSunlightTask.cpp:28-90 -> kMesh).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import batch
+from .mesher import Context, library
+
+EDIT_DTYPE = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("block", "<u4")])
+
+
+class _Desc(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in ("nx", "ny", "nz", "cx0", "cy0", "cz0")]
+
+
+def _bind(lib):
+    if getattr(lib, "_world_bound", False):
+        return lib
+    vp, P = ctypes.c_void_p, ctypes.POINTER
+    lib.hc_world_create.argtypes = [vp, vp, P(_Desc), vp, P(vp)]
+    lib.hc_world_destroy.argtypes = [vp]
+    lib.hc_world_destroy.restype = None
+    lib.hc_world_apply_edits.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_int, vp]
+    lib.hc_world_remesh.argtypes = [vp, P(batch._Arena), vp, ctypes.c_uint32, P(ctypes.c_uint32),
+                                    P(ctypes.c_uint64), P(ctypes.c_uint32), vp]
+    lib._world_bound = True
+    return lib
+
+
+class ResidentWorld:
+    """A generated world (worldgen.World) resident in a device pool, slot = chunk index."""
+
+    def __init__(self, ctx: Context, world):
+        self.ctx, self.world = ctx, world
+        self.lib = _bind(batch._bind(library()))
+        self.pool = batch.Pool(ctx, world.n_chunks)
+        self.pool.upload(0, world.blocks, world.heights)
+        slots = np.arange(world.n_chunks, dtype=np.int32)
+        h = ctypes.c_void_p()
+        desc = _Desc(world.nx, world.ny, world.nz, *world.origin)
+        ctx.check(self.lib.hc_world_create(ctx.handle, self.pool.handle, ctypes.byref(desc), slots.ctypes.data,
+                                           ctypes.byref(h)), "hc_world_create")
+        self.handle = h
+
+    def apply_edits(self, edits: np.ndarray, stream=None):
+        """edits: structured array of EDIT_DTYPE (host) or a torch int32 (n, 4) cuda tensor."""
+        if hasattr(edits, "data_ptr"):
+            self.ctx.check(self.lib.hc_world_apply_edits(self.handle, edits.data_ptr(), edits.shape[0], 1, stream),
+                           "hc_world_apply_edits")
+        else:
+            e = np.ascontiguousarray(edits, EDIT_DTYPE)
+            self.ctx.check(self.lib.hc_world_apply_edits(self.handle, e.ctypes.data, len(e), 0, stream),
+                           "hc_world_apply_edits")
+
+    def remesh(self, arena: batch.Arena, stream=None):
+        """Relights + meshes the marked chunks into arena; returns (cells, quads, meshes)."""
+        cells = np.empty(self.world.n_chunks, np.int32)
+        n, q, m = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint32()
+        a = arena.c()
+        self.ctx.check(self.lib.hc_world_remesh(self.handle, ctypes.byref(a), cells.ctypes.data, len(cells),
+                                                ctypes.byref(n), ctypes.byref(q), ctypes.byref(m), stream),
+                       "hc_world_remesh")
+        return cells[:n.value].copy(), q.value, m.value
+
+    def download(self):
+        return batch.pool_download(self.pool, 0, self.world.n_chunks)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.hc_world_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+
+def edit_world(seed: int = 12314524):
+    """Edit workload: 7 x 5 x 7 chunks of the single-chunk terrain (chunk y -2..2) so every edited
+    chunk has its neighbours."""
+    from . import worldgen
+    return worldgen.generate(7, 5, 7, (-3, -2, -3), seed=seed, caves=False, leaves_permille=50)
+
+
+def seeded_edits(n: int = 4096, seed: int = 7, centre=(16, 16, 16), radius: int = 48) -> np.ndarray:
+    """n edits uniform in the ball of `radius` voxels around `centre`: half place stone (1), half set
+    air (0), and 10% of all edits place glowstone (24) instead."""
+    rng = np.random.default_rng(seed)
+    pts = []
+    while sum(len(p) for p in pts) < n:
+        c = rng.integers(-radius, radius + 1, size=(4 * n, 3))
+        pts.append(c[(c ** 2).sum(1) <= radius * radius])
+    p = np.concatenate(pts)[:n] + np.asarray(centre)
+    kind = rng.random(n)
+    block = np.where(kind < 0.5, 1, 0).astype(np.uint32)
+    block[rng.random(n) < 0.1] = 24
+    out = np.empty(n, EDIT_DTYPE)
+    out["x"], out["y"], out["z"], out["block"] = p[:, 0], p[:, 1], p[:, 2], block
+    return out

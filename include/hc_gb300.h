@@ -121,6 +121,10 @@ hc_status hc_pool_buffers(const hc_pool *pool, uint16_t **blocks, int8_t **heigh
 hc_status hc_pool_upload(hc_pool *pool, uint32_t first, uint32_t count, const uint16_t *blocks, const int8_t *heights,
                          int src_on_device, void *stream);
 
+/* Copies slots [first, first + count) back to host or device memory (dst_on_device). Synchronous. */
+hc_status hc_pool_download(hc_pool *pool, uint32_t first, uint32_t count, uint16_t *blocks, int8_t *heights,
+                           int dst_on_device, void *stream);
+
 /* Arena that receives a batch's meshes (all pointers on the device). Chunk i of the batch gets
  * results[5*i .. 5*i+4] = {opaque quads, transparent quads, first mesh, mesh count, status}
  * (status 0 = ok, 1 = arena full, 2 = bad neighbour slot); its meshes are meshes[first ..
@@ -157,6 +161,48 @@ hc_status hc_batch_plan_result(hc_batch_plan *plan, uint64_t *quads, uint32_t *m
 hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t meshes, uint32_t *vertices,
                                  uint16_t *indices, hc_mesh_desc *mesh_descs, uint32_t *results);
 
+
+
+/* ----------------------------------------------------------------------------------------------
+ * Block edits on a resident world, then relight + remesh of the chunks they touch.
+ *
+ * Replaces the reference's edit task chain: ChunkTaskRunner<kSetBlock>::Run
+ * (client/src/ChunkSetBlockTask.cpp:37-131), the sunlight-height recomputation of
+ * ChunkTaskRunner<kFloodSunlight>::Run (client/src/ChunkFloodSunlightTask.cpp:33-66) and
+ * ChunkTaskRunner<kSetSunlight>::Run (client/src/ChunkSetSunlightTask.cpp:28-90), followed by the
+ * kMesh runs they trigger. A world is a dense grid of chunk positions over a pool.
+ * ---------------------------------------------------------------------------------------------- */
+typedef struct hc_world hc_world;
+typedef struct hc_world_desc {
+	int32_t nx, ny, nz;    /* grid size in chunks */
+	int32_t cx0, cy0, cz0; /* chunk coordinate of grid cell (0, 0, 0) */
+} hc_world_desc;
+/* One edit: world voxel coordinates and the new raw block (low 16 bits of `block`). */
+typedef struct hc_edit {
+	int32_t x, y, z;
+	uint32_t block;
+} hc_edit;
+
+/* Grid cell (ix, iy, iz), index ix + nx * (iz + nz * iy), holds chunk (cx0 + ix, cy0 + iy, cz0 + iz)
+ * in pool slot slots[index] (host array), or -1 when that chunk is not resident. */
+hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc, const int32_t *slots, hc_world **out);
+void hc_world_destroy(hc_world *world);
+
+/* Applies `n` edits in order (the last edit of a voxel wins; edits outside the resident world are
+ * ignored), recomputes the sunlight heights of every edited column with the reference's rule
+ * (a chunk's column is dark, 32, when the chunk above has a positive height there, else one above
+ * its highest block that stops vertical light; the top grid layer counts as lit from above),
+ * cascading down, and marks for remeshing every chunk whose light window holds a changed block
+ * (ChunkShouldRemesh, client/include/client/ChunkMeshTask.inl:9-15) and the 27 chunks around
+ * every chunk whose heights changed. `edits` is a host or device array (src_on_device). */
+hc_status hc_world_apply_edits(hc_world *world, const hc_edit *edits, uint32_t n, int src_on_device, void *stream);
+
+/* Relights and meshes every marked chunk whose 26 neighbours are resident (the reference's kMesh
+ * waits for them too), in grid order, into `arena` (chunk i of the batch = cells[i]); clears their
+ * marks. cells (host, capacity cap) receives the grid indices; *n_remeshed their number. On
+ * HC_ERR_CAPACITY nothing is cleared and *n_remeshed holds the number of chunks waiting. */
+hc_status hc_world_remesh(hc_world *world, const hc_batch_arena *arena, int32_t *cells, uint32_t cap,
+                          uint32_t *n_remeshed, uint64_t *quads, uint32_t *meshes, void *stream);
 
 /* ----------------------------------------------------------------------------------------------
  * Batched meshing that allocates nothing. No counterpart in the reference.

@@ -1,0 +1,77 @@
+"""Edit pipeline on the device against the CPU restatement of the reference's task chain
+(SetBlock -> FloodSunlight -> SetSunlight -> kMesh): final blocks and heights, the set of remeshed
+chunks, and byte-exact meshes of every remeshed chunk."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _meshes_of_chunk(oracle, w, cell):
+    nb = w.neighbours(*w.coords(int(cell)))
+    return oracle.mesh_chunk([w.blocks[k] for k in nb], [w.heights[k] for k in nb])
+
+
+def _run(ctx, oracle, edits, world_factory):
+    from hypercraft_gb300 import batch, world as hw
+    from oracle import edits as oe
+    w_gpu = world_factory()
+    w_ref = world_factory()
+    before = {int(c): _meshes_of_chunk(oracle, w_ref, c) for c in w_ref.meshable()}
+    dirty_ref = oe.apply_edits(w_ref, edits)
+
+    rw = hw.ResidentWorld(ctx, w_gpu)
+    rw.apply_edits(edits)
+    arena = batch.Arena(4_000_000, 8192, w_gpu.n_chunks)
+    cells, q, m = rw.remesh(arena)
+    b, h = rw.download()
+    assert np.array_equal(b, w_ref.blocks), "final blocks differ"
+    assert np.array_equal(h, w_ref.heights), "final sunlight heights differ"
+
+    meshable = set(int(c) for c in w_ref.meshable())
+    got = set(int(c) for c in cells)
+    assert list(cells) == sorted(cells), "remesh order is grid order"
+    assert got <= dirty_ref & meshable
+    for c in (dirty_ref & meshable) - got:  # the reference would remesh these too, to the same meshes
+        assert all(a == b for a, b in zip(before[c], _meshes_of_chunk(oracle, w_ref, c)))
+    host = arena.host()
+    for i, c in enumerate(cells):
+        want = _meshes_of_chunk(oracle, w_ref, c)
+        got_m = arena.chunk_meshes(i, host)
+        assert len(got_m) == len(want) and all(a == b for a, b in zip(got_m, want)), int(c)
+    # every chunk whose mesh changed was remeshed
+    for c in meshable - got:
+        assert all(a == b for a, b in zip(before[c], _meshes_of_chunk(oracle, w_ref, c))), c
+    # a second remesh with no new edits has nothing to do
+    cells2, _, _ = rw.remesh(arena)
+    assert len(cells2) == 0
+    return len(cells)
+
+
+def test_seeded_edits_match_reference_chain(ctx, oracle):
+    from hypercraft_gb300 import world as hw
+    n = _run(ctx, oracle, hw.seeded_edits(4096, seed=7), hw.edit_world)
+    assert n > 10
+
+
+def test_repeated_and_reverted_edits(ctx, oracle):
+    from hypercraft_gb300 import world as hw
+    w = hw.edit_world()
+    e = hw.seeded_edits(600, seed=11)
+    # the same voxels edited again: some reverted to their original block, some changed twice
+    again = e[:300].copy()
+    orig = np.array([w.blocks[((x >> 5) + 3) + 7 * (((z >> 5) + 3) + 7 * ((y >> 5) + 2)),
+                              (x & 31) + ((y & 31) * 32 + (z & 31)) * 32] for x, y, z in
+                     zip(again["x"], again["y"], again["z"])], np.uint32)
+    again["block"][:150] = orig[:150]
+    again["block"][150:] = 9  # glass
+    edits = np.concatenate([e, again, e[:50]])
+    _run(ctx, oracle, edits, hw.edit_world)
+
+
+def test_edits_outside_the_world_are_ignored(ctx, oracle):
+    from hypercraft_gb300 import world as hw
+    e = hw.seeded_edits(64, seed=3)
+    far = e.copy()
+    far["y"] += 10_000
+    _run(ctx, oracle, np.concatenate([e, far]), hw.edit_world)

@@ -87,3 +87,29 @@ def test_light_window_shape_and_range(oracle):
     light = oracle.relight_window(b, h)
     assert light.shape == (62 ** 3,)
     assert (light & 15).max() <= 15 and (light >> 4).max() <= 15
+
+
+def test_edit_chain_marks_every_changed_mesh(oracle):
+    """The restated SetBlock -> FloodSunlight -> SetSunlight rules mark every chunk whose mesh
+    changes (checked by meshing every chunk before and after)."""
+    from hypercraft_gb300 import world as hw
+    from oracle import edits as oe
+    w = hw.edit_world()
+    def mesh(c):
+        nb = w.neighbours(*w.coords(int(c)))
+        return oracle.mesh_chunk([w.blocks[k] for k in nb], [w.heights[k] for k in nb])
+    meshable = [int(c) for c in w.meshable()]
+    before = {c: mesh(c) for c in meshable}
+    dirty = oe.apply_edits(w, hw.seeded_edits(1024, seed=5))
+    changed = {c for c in meshable if not (len(before[c]) == len(after := mesh(c)) and
+                                           all(a == b for a, b in zip(before[c], after)))}
+    assert changed, "the edits change some meshes"
+    assert changed <= dirty
+
+
+def test_seeded_edits_are_deterministic():
+    from hypercraft_gb300 import world as hw
+    a, b = hw.seeded_edits(4096, seed=7), hw.seeded_edits(4096, seed=7)
+    assert np.array_equal(a, b)
+    d = np.sqrt((a["x"] - 16.0) ** 2 + (a["y"] - 16.0) ** 2 + (a["z"] - 16.0) ** 2)
+    assert d.max() <= 48 and 0.05 < np.mean(a["block"] == 24) < 0.15
