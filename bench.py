@@ -36,7 +36,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="scale", choices=["scale", "mixture"])
+    ap.add_argument("--workload", default="scale", choices=["scale", "mixture", "edits"])
     ap.add_argument("--size", default="", help="override grid as NXxNYxNZ (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-chunk form (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -367,6 +367,55 @@ def ours(args):
         dist.destroy_process_group()
 
 
+def edits_bench(args):
+    """Edit workload: 4,096 seeded edits (half stone, half air, 10% glowstone, within 48 voxels of the
+    centre) on 7 x 5 x 7 chunks of terrain; a step applies them, recomputes the sunlight heights and
+    relights + remeshes every chunk they touch. The world is restored (outside the timed region)
+    before each step."""
+    import torch
+    from hypercraft_gb300 import batch, mesher, world as hw
+    from hypercraft_gb300.build import build
+    from oracle import bind
+    build()
+    ctx = mesher.Context(0)
+    w = hw.edit_world()
+    edits = hw.seeded_edits(4096, seed=7)
+    rw = hw.ResidentWorld(ctx, w)
+    arena = batch.Arena(4_000_000, 8192, w.n_chunks)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sp = ctypes_stream(stream)
+    times, cells = [], None
+    for step in range(args.warmup + args.steps):
+        rw.pool.upload(0, w.blocks, w.heights, sp)
+        rw.remesh(arena, sp)  # nothing marked: clears nothing
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rw.apply_edits(edits, sp)
+        cells, quads, meshes = rw.remesh(arena, sp)
+        torch.cuda.synchronize()
+        if step >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    ms = 1e3 * float(np.median(times))
+    # CPU: the reference's kMesh runner over the same remeshed chunks, all host cores
+    wc = hw.edit_world()
+    from oracle import edits as oe
+    oe.apply_edits(wc, edits)
+    nbr = wc.neighbour_table(cells)
+    threads = os.cpu_count()
+    ref = bind.reference()
+    runner, kind = (ref, "reference") if ref is not None else (bind.oracle(), "port")
+    dt, q, _ = cpu_run(wc, cells, nbr, runner, threads)
+    line = {"metric": "edits/s", "value": len(edits) / (ms / 1e3), "unit": "edits/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "workload": "edits: 4096 seeded edits within 48 voxels of the centre of 7x5x7 terrain chunks",
+            "remeshed_chunks_per_step": int(len(cells)), "quads_per_step": int(quads),
+            "remesh_latency_ms": ms,
+            "cpu_baseline": {"value": len(edits) / dt, "unit": "edits/s", "cores": threads, "kind": kind,
+                             "sample": f"kMesh of the same {len(cells)} chunks ({dt * 1e3:.1f} ms), edit application excluded"}}
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_stream(stream):
     import ctypes
     return ctypes.c_void_p(stream.cuda_stream)
@@ -374,6 +423,9 @@ def ctypes_stream(stream):
 
 def main():
     args = parse()
+    if args.workload == "edits":
+        edits_bench(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
     else:

@@ -51,6 +51,7 @@ enum : uint8_t {
 	kFDirect = 2,     // vertical pass or no solid collision (AO does not darken)
 	kFVertical = 4,   // transparency == transparent
 	kFOpaqueCube = 8, // six non-empty, non-transparent textures and no custom mesh
+	                  // (kFIndirect and kFDirect are also bits 7 and 6 of the class id itself)
 	kFEmpty = 16,     // six empty textures and no custom mesh
 	kFTagShift = 5    // 2-bit id tag
 };
@@ -97,18 +98,19 @@ __constant__ int8_t c_corner[6][4][3][3] = {
      {{0, -1, -1}, {1, -1, -1}, {1, 0, -1}}}};
 
 // Shared memory of one chunk CTA (about 215 KB: one CTA per SM).
+constexpr int kRowWords = (kWinRows + 31) / 32;
 struct Relight {
 	uint64_t pass[kWinRows];   // blocks light may enter
 	ulonglong2 lit[kWinRows];  // current level set: .x sun, .y torch
-	uint32_t low_rows[(kWinRows + 31) / 32]; // rows holding emitters of level 1..14
+	uint32_t low_rows[kRowWords]; // rows holding emitters of level 1..14
+	uint32_t changed[2][kRowWords]; // rows that changed at the last two levels
 };
 struct Smem {
 	DevClass classes[256];
 	const uint16_t *blk[27];
 	const int8_t *hgt[27];
 	const uint32_t *pln[27]; // per-chunk bit planes, or null (then the window is seeded from blocks)
-	alignas(16) uint8_t cls[kClsCells + 8];
-	alignas(16) uint8_t light[kLtCells + 8];
+	alignas(16) uint16_t cell[kClsCells + 8]; // per cell of [-1, 32]^3: light (low byte), class id (high byte)
 	union {
 		Relight rl;
 		uint32_t masks[kPlanes][32][4]; // per plane row: visible, equal-right, equal-below, transparent pass
@@ -164,7 +166,11 @@ __device__ __forceinline__ bool show(uint16_t a, uint16_t b) {
 	return !ta || tb || tex_liquid(b);
 }
 
-__device__ __forceinline__ uint8_t class_at(const Smem &S, int x, int y, int z) { return S.cls[cls_index(x, y, z)]; }
+__device__ __forceinline__ uint8_t class_at(const Smem &S, int x, int y, int z) { return S.cell[cls_index(x, y, z)] >> 8; }
+// Class ids carry the two light-pass flags: bit 7 = light may pass (kFIndirect), bit 6 = does not
+// darken ambient occlusion (kFDirect).
+__device__ __forceinline__ bool id_indirect(uint32_t c) { return (c >> 7) & 1u; }
+__device__ __forceinline__ bool id_direct(uint32_t c) { return (c >> 6) & 1u; }
 __device__ __forceinline__ uint8_t tag_of(const DevClass &k) { return k.flags >> kFTagShift; }
 
 // Dynamic face textures of a flowing liquid at (x, y, z) in [-1, 32]^3.
@@ -231,21 +237,20 @@ __constant__ int16_t c_corner_off[6][4][3] = {
 
 __device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
 	const int base = cls_index(x, y, z);
-	const int fi = base + c_front_off[face];
-	const bool dp3 = S.classes[S.cls[fi]].flags & kFDirect;
-	const uint8_t lf = S.light[fi];
+	const uint32_t cf = S.cell[base + c_front_off[face]];
+	const bool dp3 = id_direct(cf >> 8);
+	const uint32_t lf = cf & 0xffu;
 	Light4 r{0, 0, 0};
 #pragma unroll
 	for (int v = 0; v < 4; ++v) {
 		bool ip[3], dp[3];
-		uint8_t l[3];
+		uint32_t l[3];
 #pragma unroll
 		for (int b = 0; b < 3; ++b) {
-			const int ci = base + c_corner_off[face][v][b];
-			const uint8_t fl = S.classes[S.cls[ci]].flags;
-			ip[b] = fl & kFIndirect;
-			dp[b] = fl & kFDirect;
-			l[b] = S.light[ci];
+			const uint32_t c = S.cell[base + c_corner_off[face][v][b]];
+			ip[b] = id_indirect(c >> 8);
+			dp[b] = id_direct(c >> 8);
+			l[b] = c & 0xffu;
 		}
 		const int blocked = !dp[0] + !dp[1] + !dp[2] + !dp3;
 		const uint32_t ao = ((!dp[0] && !dp[2]) || (!dp[1] && !dp3)) ? 0u : (uint32_t)(3 - blocked > 0 ? 3 - blocked : 0);

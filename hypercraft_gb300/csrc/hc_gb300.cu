@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_relight_single(Refs27 refs, Dev
 	relight_window(S, T);
 	__syncthreads();
 	for (int i = threadIdx.x; i < kLtCells; i += kThreads)
-		light34[i] = S.light[i];
+		light34[i] = (uint8_t)(S.cell[i] & 0xffu);
 }
 
 enum : uint32_t { kChunkBadSlot = 2 };
@@ -132,19 +132,48 @@ __device__ void bad_item(const Arena &A, uint32_t item, unsigned int *failed) {
 	}
 }
 
-// Batched form: a persistent grid; each CTA takes the next chunk from a device work counter.
+// Starts an asynchronous copy of [p, p + bytes) into L2 (bytes a multiple of 16, p 16-byte aligned).
+__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
+	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Prefetches what the next chunk of a batch reads first: its own blocks and the 27 chunks' planes.
+__device__ __forceinline__ void prefetch_item(const uint16_t *pool_blocks, const uint32_t *pool_planes, uint32_t pool_cap,
+                                              const int32_t *nbr, uint32_t item) {
+	const int t = threadIdx.x;
+	if (t < 27) {
+		const int32_t slot = nbr[(size_t)item * 27 + t];
+		if (slot >= 0 && (uint32_t)slot < pool_cap) {
+			if (pool_planes)
+				prefetch_l2(pool_planes + (size_t)slot * kPlaneStride, kPlaneStride * sizeof(uint32_t));
+			if (t == 26)
+				for (int q = 0; q < 4; ++q)
+					prefetch_l2(pool_blocks + (size_t)slot * 32768 + q * 8192, 16384);
+		}
+	}
+}
+
+// Batched form: a persistent grid; each CTA takes chunks from a device work counter, claiming the
+// next one while it meshes the current one so that the next chunk's data is already in L2.
 __global__ void __launch_bounds__(kThreads, 1)
     k_mesh_batch(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
                  const int32_t *nbr, uint32_t n, unsigned int *work, unsigned int *failed, DevTables T, Arena A) {
 	Smem &S = smem();
-	__shared__ uint32_t s_item;
+	__shared__ uint32_t s_next;
+	if (threadIdx.x == 0)
+		s_next = atomicAdd(work, 1u);
+	__syncthreads();
+	uint32_t item = s_next;
 	for (;;) {
-		if (threadIdx.x == 0)
-			s_item = atomicAdd(work, 1u);
-		__syncthreads();
-		const uint32_t item = s_item;
 		if (item >= n)
 			break;
+		__syncthreads(); // everyone has read s_next
+		if (threadIdx.x == 0)
+			s_next = atomicAdd(work, 1u);
+		__syncthreads();
+		const uint32_t next = s_next;
+		if (next < n)
+			prefetch_item(pool_blocks, pool_planes, pool_cap, nbr, next);
 		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item)) {
 			mesh_chunk_cta(S, T, A, item);
 			if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
@@ -153,6 +182,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 			bad_item(A, item, failed);
 		}
 		__syncthreads();
+		item = next;
 	}
 }
 
@@ -240,7 +270,9 @@ hc_status fail(hc_ctx *ctx, hc_status s, const std::string &msg) {
 // Derives the block classes from the registry: each distinct device row gets one id.
 bool build_classes(const hc_registry &reg, std::vector<uint8_t> &class_of, std::vector<DevClass> &classes) {
 	class_of.assign(65536, 0);
-	classes.clear();
+	classes.assign(256, DevClass{});
+	std::vector<bool> used(256, false);
+	uint32_t group_count[4] = {0, 0, 0, 0};
 	std::map<std::string, uint8_t> seen;
 	for (uint32_t raw = 0; raw < 65536u; ++raw) {
 		const hc_block_props &p = reg.props[raw];
@@ -278,14 +310,20 @@ bool build_classes(const hc_registry &reg, std::vector<uint8_t> &class_of, std::
 		std::string key(reinterpret_cast<const char *>(&d), sizeof(d));
 		auto it = seen.find(key);
 		if (it == seen.end()) {
-			if (classes.size() >= 256)
+			// the id carries the light-pass flags: bit 7 indirect, bit 6 direct, 64 ids per pair
+			const uint32_t group = ((flags & kFIndirect) ? 2u : 0u) | ((flags & kFDirect) ? 1u : 0u);
+			if (group_count[group] >= 64)
 				return false;
-			it = seen.emplace(key, (uint8_t)classes.size()).first;
-			classes.push_back(d);
+			const uint8_t id = (uint8_t)((group << 6) | group_count[group]++);
+			it = seen.emplace(key, id).first;
+			classes[id] = d;
+			used[id] = true;
 		}
 		class_of[raw] = it->second;
 	}
-	classes.resize(256, classes[0]);
+	for (int i = 0; i < 256; ++i)
+		if (!used[i])
+			classes[i] = classes[class_of[0]];
 	return true;
 }
 
@@ -1092,21 +1130,27 @@ bool noalloc_build_tables() {
 	if (g_noalloc_tables_built)
 		return true;
 	hc_registry_build(&g_noalloc_registry);
-	uint32_t n = 0;
+	// same id scheme as the context tables: bit 7 indirect pass, bit 6 direct pass, 64 ids per pair
+	uint32_t count[4] = {0, 0, 0, 0};
+	bool used[256] = {false};
 	for (uint32_t raw = 0; raw < 65536u; ++raw) {
 		const DevClass d = noalloc_class_row(g_noalloc_registry.props[raw]);
+		const uint32_t group = ((d.flags & kFIndirect) ? 2u : 0u) | ((d.flags & kFDirect) ? 1u : 0u);
 		uint32_t c = 0;
-		while (c < n && std::memcmp(&g_noalloc_classes_host[c], &d, sizeof(d)) != 0)
+		while (c < count[group] && std::memcmp(&g_noalloc_classes_host[(group << 6) | c], &d, sizeof(d)) != 0)
 			++c;
-		if (c == n) {
-			if (n == 256)
+		if (c == count[group]) {
+			if (c == 64)
 				return false;
-			g_noalloc_classes_host[n++] = d;
+			g_noalloc_classes_host[(group << 6) | c] = d;
+			used[(group << 6) | c] = true;
+			++count[group];
 		}
-		g_noalloc_class_of_host[raw] = (uint8_t)c;
+		g_noalloc_class_of_host[raw] = (uint8_t)((group << 6) | c);
 	}
-	for (uint32_t c = n; c < 256; ++c)
-		g_noalloc_classes_host[c] = g_noalloc_classes_host[0];
+	for (uint32_t c = 0; c < 256; ++c)
+		if (!used[c])
+			g_noalloc_classes_host[c] = g_noalloc_classes_host[g_noalloc_class_of_host[0]];
 	g_noalloc_tables_built = true;
 	return true;
 }

@@ -67,7 +67,7 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 		S.classes[i] = T.classes[i];
 	__syncthreads();
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	constexpr int kRows = kCls * kCls, kBatch = 4; // 1156 rows
+	constexpr int kRows = kCls * kCls, kBatch = 4; // 1156 rows = 289 batches
 	static_assert(kRows % kBatch == 0, "row batches");
 	bool content = false, open = false;
 	for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
@@ -87,10 +87,10 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 #pragma unroll
 		for (int j = 0; j < kBatch; ++j) {
 			const int row = row0 + j, y = row / kCls - 1, z = row % kCls - 1;
-			uint8_t *dst = S.cls + row * kCls;
-			dst[lane + 1] = c[j];
+			uint16_t *dst = S.cell + row * kCls;
+			dst[lane + 1] = (uint16_t)(c[j] << 8);
 			if (lane < 2)
-				dst[lane ? kCls - 1 : 0] = ce[j];
+				dst[lane ? kCls - 1 : 0] = (uint16_t)(ce[j] << 8);
 			const uint8_t f = S.classes[c[j]].flags, fe = S.classes[ce[j]].flags;
 			const uint32_t oc = __ballot_sync(0xffffffffu, f & kFOpaqueCube);
 			const uint32_t em = __ballot_sync(0xffffffffu, f & kFEmpty);
@@ -192,7 +192,7 @@ __device__ void custom_emit(Smem &S, const Emit &E, int first, uint32_t ko, uint
 				op[cur_axis] -= d;
 				ne[cur_axis] += d;
 				lo = light4(S, cur_face, op[0], op[1], op[2]);
-				if (S.classes[class_at(S, ne[0], ne[1], ne[2])].flags & kFIndirect)
+				if (id_indirect(class_at(S, ne[0], ne[1], ne[2])))
 					hi = light4(S, cur_face, x, y, z);
 				else
 					hi = lo;

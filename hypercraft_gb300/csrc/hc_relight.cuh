@@ -27,6 +27,9 @@ __device__ __forceinline__ uint64_t dist_mask_rem(int rem) {
 	return ((~0ull) >> (63 - hi)) & ~((1ull << lo) - 1ull);
 }
 
+// The light of [-1, 32]^3 lives in the low byte of each staged cell (little-endian).
+__device__ __forceinline__ uint8_t *light_bytes(Smem &S) { return reinterpret_cast<uint8_t *>(S.cell); }
+
 // Writes level `t` into the light nibble of newly lit cells of row (wy, wz) inside [-1, 32]^3.
 __device__ __forceinline__ void write_new(uint8_t *light, int wy, int wz, uint64_t bits, uint32_t t, int shift) {
 	if (wy < 14 || wy > 47 || wz < 14 || wz > 47)
@@ -36,7 +39,7 @@ __device__ __forceinline__ void write_new(uint8_t *light, int wy, int wz, uint64
 	while (bits) {
 		int b = __ffsll((long long)bits) - 1;
 		bits &= bits - 1;
-		light[row + b - 14] |= (uint8_t)(t << shift);
+		light[2 * (row + b - 14)] |= (uint8_t)(t << shift);
 	}
 }
 
@@ -44,11 +47,11 @@ __device__ __forceinline__ void write_new(uint8_t *light, int wy, int wz, uint64
 __device__ __forceinline__ void write_row15(uint8_t *light, int wy, int wz, uint64_t sun, uint64_t torch) {
 	if (wy < 14 || wy > 47 || wz < 14 || wz > 47)
 		return;
-	uint8_t *row = light + ((wy - 14) * kLt + (wz - 14)) * kLt;
+	uint8_t *row = light + 2 * ((wy - 14) * kLt + (wz - 14)) * kLt;
 	const uint64_t s = sun >> 14, t = torch >> 14;
 #pragma unroll
 	for (int i = 0; i < kLt; ++i)
-		row[i] = (uint8_t)((((s >> i) & 1u) ? 0x0fu : 0u) | (((t >> i) & 1u) ? 0xf0u : 0u));
+		row[2 * i] = (uint8_t)((((s >> i) & 1u) ? 0x0fu : 0u) | (((t >> i) & 1u) ? 0xf0u : 0u));
 }
 
 // Seeds from the 27 chunks' bit planes: each window row joins three 32-bit chunk rows.
@@ -74,7 +77,7 @@ __device__ void seed_from_planes(Smem &S) {
 		R.lit[r] = make_ulonglong2(v[kPlaneSun], v[kPlaneT15]);
 		if (low & 1u)
 			atomicOr(&R.low_rows[r >> 5], 1u << (r & 31));
-		write_row15(S.light, wy, wz, v[kPlaneSun], v[kPlaneT15]);
+		write_row15(light_bytes(S), wy, wz, v[kPlaneSun], v[kPlaneT15]);
 	}
 }
 
@@ -113,15 +116,18 @@ __device__ void seed_from_blocks(Smem &S, const DevTables &T) {
 	for (int r = threadIdx.x; r < kWinRows; r += kThreads) {
 		const int wy = r / kWin, wz = r - wy * kWin;
 		const ulonglong2 l = R.lit[r];
-		write_row15(S.light, wy, wz, l.x, l.y);
+		write_row15(light_bytes(S), wy, wz, l.x, l.y);
 	}
 }
+
+// Bit of row r in a row bitmap.
+__device__ __forceinline__ bool row_bit(const uint32_t *m, int r) { return (m[r >> 5] >> (r & 31)) & 1u; }
 
 __device__ void relight_window(Smem &S, const DevTables &T) {
 	Relight &R = S.u.rl;
 	const int tid = threadIdx.x;
-	for (int i = tid; i < (kWinRows + 31) / 32; i += kThreads)
-		R.low_rows[i] = 0;
+	for (int i = tid; i < kRowWords; i += kThreads)
+		R.low_rows[i] = 0, R.changed[0][i] = 0, R.changed[1][i] = 0;
 	__syncthreads();
 	if (S.pln[26])
 		seed_from_planes(S);
@@ -129,6 +135,10 @@ __device__ void relight_window(Smem &S, const DevTables &T) {
 		seed_from_blocks(S, T);
 	__syncthreads();
 
+	// A row can gain cells at level t only when it or one of its four neighbour rows changed at
+	// level t + 1: otherwise its dilation is the one it already saw, while the distance mask only
+	// shrinks. So after the first level only rows next to the last changes (the light front) and
+	// rows holding emitters of the level are visited.
 	constexpr int kRowsPerThread = (kWinRows + kThreads - 1) / kThreads;
 	int rem0[kRowsPerThread]; // t - 1 - dist(y, z) = t + rem0
 #pragma unroll
@@ -137,17 +147,31 @@ __device__ void relight_window(Smem &S, const DevTables &T) {
 		const int wy = r / kWin, wz = r - wy * kWin;
 		rem0[k] = r < kWinRows ? -1 - axis_dist(wy - 15) - axis_dist(wz - 15) : -1000;
 	}
+	uint8_t *light = light_bytes(S);
 	for (int t = 14; t >= 1; --t) {
+		const uint32_t *prev = R.changed[(t + 1) & 1];
+		uint32_t *cur_chg = R.changed[t & 1];
+		for (int i = tid; i < kRowWords; i += kThreads)
+			cur_chg[i] = 0; // last read at level t + 1
 		uint64_t ns[kRowsPerThread], nt[kRowsPerThread];
 		uint32_t changed = 0;
 #pragma unroll
 		for (int k = 0; k < kRowsPerThread; ++k) {
 			const int r = tid + k * kThreads;
 			const int rem = t + rem0[k];
-			const bool low = r < kWinRows && ((R.low_rows[r >> 5] >> (r & 31)) & 1u);
+			if (r >= kWinRows)
+				continue;
+			const bool low = row_bit(R.low_rows, r);
 			if (rem < 0 && !low)
 				continue;
 			const int wy = r / kWin, wz = r - wy * kWin;
+			if (t < 14 && !low) {
+				const bool near = row_bit(prev, r) || (wz > 0 && row_bit(prev, r - 1)) ||
+				                  (wz < kWin - 1 && row_bit(prev, r + 1)) || (wy > 0 && row_bit(prev, r - kWin)) ||
+				                  (wy < kWin - 1 && row_bit(prev, r + kWin));
+				if (!near)
+					continue;
+			}
 			const ulonglong2 cur = R.lit[r];
 			uint64_t s = cur.x, tt = cur.y;
 			if (rem >= 0) {
@@ -195,8 +219,9 @@ __device__ void relight_window(Smem &S, const DevTables &T) {
 			const int wy = r / kWin, wz = r - wy * kWin;
 			const ulonglong2 cur = R.lit[r];
 			R.lit[r] = make_ulonglong2(ns[k], nt[k]);
-			write_new(S.light, wy, wz, ns[k] & ~cur.x, (uint32_t)t, 0);
-			write_new(S.light, wy, wz, nt[k] & ~cur.y, (uint32_t)t, 4);
+			atomicOr(&cur_chg[r >> 5], 1u << (r & 31));
+			write_new(light, wy, wz, ns[k] & ~cur.x, (uint32_t)t, 0);
+			write_new(light, wy, wz, nt[k] & ~cur.y, (uint32_t)t, 4);
 		}
 		__syncthreads();
 	}
