@@ -29,6 +29,7 @@ def _bind(lib):
         return lib
     vp, P = ctypes.c_void_p, ctypes.POINTER
     lib.hc_pool_create.argtypes = [vp, ctypes.c_uint32, P(vp)]
+    lib.hc_pool_download.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, ctypes.c_int, vp]
     lib.hc_pool_destroy.argtypes = [vp]
     lib.hc_pool_destroy.restype = None
     lib.hc_pool_capacity.argtypes = [vp]
@@ -108,6 +109,10 @@ class Arena:
                                  bool(d["transparent"])))
         return out
 
+    def results_host(self, n: int) -> np.ndarray:
+        """The first n chunks' result words, (n, 5) uint32."""
+        return self.results[:5 * n].cpu().numpy().view(np.uint32).reshape(-1, 5)
+
     def host(self) -> dict:
         return {"vertices": self.vertices.cpu().numpy().view(np.uint32).reshape(-1, 2),
                 "indices": self.indices.cpu().numpy().view(np.uint16),
@@ -178,10 +183,6 @@ def upload_world(ctx: Context, world, chunks=None) -> ResidentWorld:
 def pool_download(pool: Pool, first: int, count: int):
     """Blocks (count, 32768) uint16 and heights (count, 1024) int8 of slots [first, first+count)."""
     lib = _bind(library())
-    if not hasattr(lib, "_dl_bound"):
-        lib.hc_pool_download.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p,
-                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
-        lib._dl_bound = True
     b = np.empty((count, 32768), np.uint16)
     h = np.empty((count, 1024), np.int8)
     pool.ctx.check(lib.hc_pool_download(pool.handle, first, count, b.ctypes.data, h.ctypes.data, 0, None),

@@ -1,7 +1,8 @@
 """Builds the in-tree shared libraries (nvcc for sm_103a, g++ for host code).
 
 ``build()`` compiles, in parallel:
-  * ``_lib/libhc_gb300.so``   the CUDA relighter + mesher behind include/hc_gb300.h;
+  * ``_lib/libhc_gb300.so``   the CUDA relighter + mesher, world stages and request server behind
+    include/hc_gb300.h;
   * ``_lib/libhc_worldgen.so`` the seeded synthetic world generator (host only).
 Each library is rebuilt only when one of its sources is newer than it.
 """
@@ -34,10 +35,12 @@ def _stale(target: str, deps) -> bool:
 def _jobs(force: bool):
     jobs = []
     gpu = os.path.join(LIB_DIR, "libhc_gb300.so")
-    gpu_deps = _sources("*.cu", "*.cuh", "*.h", "hc_registry.cpp") + [os.path.join(INCLUDE_DIR, "hc_gb300.h")]
+    gpu_deps = _sources("*.cu", "*.cuh", "*.h", "hc_registry.cpp", "hc_server.cpp") + [os.path.join(INCLUDE_DIR,
+                                                                                              "hc_gb300.h")]
     if force or _stale(gpu, gpu_deps):
         jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-                     "-o", gpu, os.path.join(CSRC_DIR, "hc_gb300.cu"), os.path.join(CSRC_DIR, "hc_registry.cpp")])
+                     "-o", gpu, os.path.join(CSRC_DIR, "hc_gb300.cu"), os.path.join(CSRC_DIR, "hc_registry.cpp"),
+                     os.path.join(CSRC_DIR, "hc_server.cpp")])
     wg = os.path.join(LIB_DIR, "libhc_worldgen.so")
     wg_deps = _sources("hc_worldgen.*", "hc_registry.*", "hc_flow.h")
     if force or _stale(wg, wg_deps):

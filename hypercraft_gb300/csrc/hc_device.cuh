@@ -110,6 +110,7 @@ struct Smem {
 	const uint16_t *blk[27];
 	const int8_t *hgt[27];
 	const uint32_t *pln[27]; // per-chunk bit planes, or null (then the window is seeded from blocks)
+	const uint8_t *lgt[27];  // per-chunk light from the batch light pass, or null (then relight the window)
 	alignas(16) uint16_t cell[kClsCells + 8]; // per cell of [-1, 32]^3: light (low byte), class id (high byte)
 	union {
 		Relight rl;

@@ -12,6 +12,7 @@
 #include "../../include/hc_gb300.h"
 #include "hc_mesh.cuh"
 #include "hc_world.cuh"
+#include "hc_internal.h"
 #include "hc_registry.h"
 
 namespace hc {
@@ -34,22 +35,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_mesh_single(Refs27 refs, DevTab
 		S.blk[threadIdx.x] = refs.blk[threadIdx.x];
 		S.hgt[threadIdx.x] = refs.hgt[threadIdx.x];
 		S.pln[threadIdx.x] = refs.pln[threadIdx.x];
+		S.lgt[threadIdx.x] = nullptr;
 	}
 	__syncthreads();
 	mesh_chunk_cta(S, T, A, 0);
-}
-
-// Bit planes of chunks: one thread per 32-cell row, 32 rows (one flag word) per warp.
-__device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hgt, const DevClass *cls_smem,
-                                           const uint8_t *class_of, int r, uint32_t *out) {
-	uint32_t pass, sun, t15;
-	const bool low = chunk_plane_row(blk, hgt, cls_smem, class_of, r >> 5, r & 31, pass, sun, t15);
-	out[kPlanePass * kPlaneWords + r] = pass;
-	out[kPlaneSun * kPlaneWords + r] = sun;
-	out[kPlaneT15 * kPlaneWords + r] = t15;
-	const uint32_t lows = __ballot_sync(0xffffffffu, low);
-	if ((threadIdx.x & 31) == 0)
-		out[3 * kPlaneWords + (r >> 5)] = lows;
 }
 
 // Planes of the listed pool slots (grid-stride over slot x row).
@@ -87,6 +76,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_relight_single(Refs27 refs, Dev
 		S.blk[threadIdx.x] = refs.blk[threadIdx.x];
 		S.hgt[threadIdx.x] = refs.hgt[threadIdx.x];
 		S.pln[threadIdx.x] = refs.pln[threadIdx.x];
+		S.lgt[threadIdx.x] = nullptr;
 	}
 	for (int i = threadIdx.x; i < 256; i += kThreads)
 		S.classes[i] = T.classes[i];
@@ -100,8 +90,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_relight_single(Refs27 refs, Dev
 enum : uint32_t { kChunkBadSlot = 2 };
 
 // Points S.blk / S.hgt at the 27 neighbour slots of batch item `item`; false if a slot is invalid.
+// With `light` (the batch light pass), S.lgt points at the 27 chunks' light, found through the batch's
+// own chunk numbering nbr_local.
 __device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes,
-                          uint32_t pool_cap, const int32_t *nbr, uint32_t item) {
+                          uint32_t pool_cap, const int32_t *nbr, uint32_t item, const uint8_t *light = nullptr,
+                          const int32_t *nbr_local = nullptr) {
 	__shared__ int s_bad;
 	if (threadIdx.x == 0)
 		s_bad = 0;
@@ -113,10 +106,12 @@ __device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *po
 			S.blk[threadIdx.x] = pool_blocks;
 			S.hgt[threadIdx.x] = pool_heights;
 			S.pln[threadIdx.x] = nullptr;
+			S.lgt[threadIdx.x] = nullptr;
 		} else {
 			S.blk[threadIdx.x] = pool_blocks + (size_t)slot * 32768;
 			S.hgt[threadIdx.x] = pool_heights + (size_t)slot * 1024;
 			S.pln[threadIdx.x] = pool_planes ? pool_planes + (size_t)slot * kPlaneStride : nullptr;
+			S.lgt[threadIdx.x] = light ? light + (size_t)nbr_local[(size_t)item * 27 + threadIdx.x] * 32768 : nullptr;
 		}
 	}
 	__syncthreads();
@@ -157,9 +152,12 @@ __device__ __forceinline__ void prefetch_item(const uint16_t *pool_blocks, const
 // next one while it meshes the current one so that the next chunk's data is already in L2.
 __global__ void __launch_bounds__(kThreads, 1)
     k_mesh_batch(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
-                 const int32_t *nbr, uint32_t n, unsigned int *work, unsigned int *failed, DevTables T, Arena A) {
+                 const int32_t *nbr, uint32_t n, const uint32_t *n_dev, unsigned int *work, unsigned int *failed,
+                 DevTables T, Arena A, const uint8_t *light, const int32_t *nbr_local) {
 	Smem &S = smem();
 	__shared__ uint32_t s_next;
+	if (n_dev) // the batch length is known on the device only (a world remesh)
+		n = *n_dev;
 	if (threadIdx.x == 0)
 		s_next = atomicAdd(work, 1u);
 	__syncthreads();
@@ -174,7 +172,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 		const uint32_t next = s_next;
 		if (next < n)
 			prefetch_item(pool_blocks, pool_planes, pool_cap, nbr, next);
-		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item)) {
+		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, light, nbr_local)) {
 			mesh_chunk_cta(S, T, A, item);
 			if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
 				atomicAdd(failed, 1u);
@@ -222,6 +220,11 @@ struct hc_batch_plan {
 	int grid = 0;
 	int32_t *d_slots = nullptr;            // distinct valid slots the batch reads (their planes are refreshed)
 	uint32_t n_slots = 0;
+	// batch light pass (persistent form): the distinct slots are the batch's chunks 0..n_slots-1
+	int32_t *d_nb6 = nullptr;       // per batch chunk: its six face neighbours in the batch, or -1
+	int32_t *d_nbr_local = nullptr; // n x 27: the neighbour table in batch chunk numbers
+	uint32_t *d_levels = nullptr;   // per batch chunk: 2 channels x 15 level planes
+	uint8_t *d_light = nullptr;     // per batch chunk: 32768 light bytes
 	unsigned long long *d_state = nullptr; // quad cursor, mesh cursor, work counter, failed chunks
 	unsigned long long *h_state = nullptr; // pinned
 	cudaGraph_t graph = nullptr;
@@ -698,6 +701,55 @@ Arena plan_arena(const hc_batch_plan *p) {
 	             p->arena.results};
 }
 
+// Numbers the batch's distinct slots 0..n_slots-1 (their order in `slots`), rewrites the neighbour
+// table in those numbers and derives every batch chunk's face neighbours from the 3x3x3 blocks of
+// the table's rows (two slots are face neighbours when some row holds both, one step apart), then
+// allocates the light pass's level planes and light bytes.
+cudaError_t plan_light_tables(hc_batch_plan *p, const std::vector<int32_t> &table, const std::vector<int32_t> &slots) {
+	const uint32_t m = (uint32_t)slots.size();
+	std::vector<int32_t> local(p->pool->capacity, -1);
+	for (uint32_t i = 0; i < m; ++i)
+		local[slots[i]] = (int32_t)i;
+	std::vector<int32_t> nbr_local(table.size(), 0), nb6((size_t)m * 6, -1);
+	const int kOff[3] = {1, -1, 0}; // neighbour index digit -> offset (common/include/common/Position.hpp:146-152)
+	const auto digit = [](int off) { return off == 1 ? 0 : (off == -1 ? 1 : 2); };
+	for (size_t row = 0; row < table.size() / 27; ++row) {
+		const int32_t *t = table.data() + row * 27;
+		bool ok = true;
+		for (int k = 0; k < 27; ++k) {
+			ok &= t[k] >= 0 && (uint32_t)t[k] < p->pool->capacity;
+			nbr_local[row * 27 + k] = ok ? local[t[k]] : 0;
+		}
+		if (!ok)
+			continue; // the mesher reports the bad slot
+		for (int k = 0; k < 27; ++k) {
+			const int o[3] = {kOff[k / 9], kOff[(k / 3) % 3], kOff[k % 3]}; // x, y, z
+			for (int f = 0; f < 6; ++f) {
+				int q[3] = {o[0], o[1], o[2]};
+				q[f >> 1] += (f & 1) ? 1 : -1;
+				if (q[0] < -1 || q[0] > 1 || q[1] < -1 || q[1] > 1 || q[2] < -1 || q[2] > 1)
+					continue;
+				const int j = digit(q[0]) * 9 + digit(q[1]) * 3 + digit(q[2]);
+				int32_t &dst = nb6[(size_t)local[t[k]] * 6 + f];
+				if (dst < 0)
+					dst = local[t[j]];
+			}
+		}
+	}
+	cudaError_t e = cudaMalloc(&p->d_nb6, nb6.size() * sizeof(int32_t));
+	if (e == cudaSuccess)
+		e = cudaMemcpy(p->d_nb6, nb6.data(), nb6.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess)
+		e = cudaMalloc(&p->d_nbr_local, nbr_local.size() * sizeof(int32_t));
+	if (e == cudaSuccess)
+		e = cudaMemcpy(p->d_nbr_local, nbr_local.data(), nbr_local.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess)
+		e = cudaMalloc(&p->d_levels, (size_t)m * kLevelSlotWords * sizeof(uint32_t));
+	if (e == cudaSuccess)
+		e = cudaMalloc(&p->d_light, (size_t)m * 32768);
+	return e;
+}
+
 hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 	hc_ctx *ctx = p->ctx;
 	HC_CUDA(ctx, cudaMemsetAsync(p->d_state, 0, 4 * sizeof(unsigned long long), st));
@@ -708,13 +760,22 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		                                     p->pool->d_planes);
 		HC_CUDA(ctx, cudaGetLastError());
 	}
+	if (p->d_light) {
+		const LightPass L{p->d_slots, p->d_nb6, p->pool->d_planes, p->pool->d_blocks, p->d_levels, p->d_light, p->n_slots};
+		const uint64_t rows = (uint64_t)p->n_slots * kPlaneWords;
+		const int blocks = (int)std::min<uint64_t>((rows + 255) / 256, (uint64_t)p->grid * 16);
+		for (int t = kLevels; t >= 1; --t) {
+			k_light_level<<<blocks, 256, 0, st>>>(L, tables(ctx), t);
+			HC_CUDA(ctx, cudaGetLastError());
+		}
+	}
 	const Arena A = plan_arena(p);
 	unsigned int *work = reinterpret_cast<unsigned int *>(p->d_state + 2);
 	unsigned int *failed = reinterpret_cast<unsigned int *>(p->d_state + 3);
 	if (p->mode == HC_BATCH_PERSISTENT) {
 		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(p->pool->d_blocks, p->pool->d_heights, p->pool->d_planes,
-		                                                          p->pool->capacity, p->nbr, p->n, work, failed,
-		                                                          tables(ctx), A);
+		                                                          p->pool->capacity, p->nbr, p->n, nullptr, work, failed,
+		                                                          tables(ctx), A, p->d_light, p->d_nbr_local);
 		HC_CUDA(ctx, cudaGetLastError());
 	} else {
 		for (uint32_t i = 0; i < p->n; ++i) {
@@ -770,6 +831,8 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 		e = cudaMalloc(&p->d_slots, std::max<size_t>(1, slots.size()) * sizeof(int32_t));
 		if (e == cudaSuccess && !slots.empty())
 			e = cudaMemcpy(p->d_slots, slots.data(), slots.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+		if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT && !slots.empty())
+			e = plan_light_tables(p, table, slots);
 	}
 	if (e == cudaSuccess)
 		e = cudaMalloc(&p->d_state, 4 * sizeof(unsigned long long));
@@ -810,6 +873,10 @@ void hc_batch_plan_destroy(hc_batch_plan *plan) {
 	if (plan->capture_stream)
 		cudaStreamDestroy(plan->capture_stream);
 	cudaFree(plan->d_slots);
+	cudaFree(plan->d_nb6);
+	cudaFree(plan->d_nbr_local);
+	cudaFree(plan->d_levels);
+	cudaFree(plan->d_light);
 	cudaFree(plan->d_state);
 	cudaFreeHost(plan->h_state);
 	delete plan;
@@ -881,24 +948,154 @@ struct hc_world {
 	hc_pool *pool = nullptr;
 	hc_world_desc desc{};
 	int cells = 0;
+	uint32_t flood_words = 0, dirty_cap = 0;
 	int32_t *d_slots = nullptr;
-	uint8_t *d_dirty = nullptr, *d_hchg = nullptr, *d_slot_mark = nullptr;
-	uint32_t *d_flood = nullptr;
+	uint32_t *d_flags = nullptr, *d_flood = nullptr, *d_stale = nullptr, *d_counts = nullptr;
+	int32_t *d_dirty_list = nullptr, *d_flood_list = nullptr, *d_hchg_list = nullptr, *d_stale_list = nullptr;
+	int32_t *d_list = nullptr, *d_nbr = nullptr;
 	hc_edit *d_edits = nullptr;
-	int32_t *d_list = nullptr, *d_nbr = nullptr, *d_slot_list = nullptr;
-	uint32_t *d_count = nullptr, *h_count = nullptr;
-	unsigned long long *d_state = nullptr, *h_state = nullptr;
+	int32_t *d_stage = nullptr;                 // staged load/unload positions and slots
+	unsigned long long *d_state = nullptr;      // arena cursors, work counter, failed count
+	uint32_t *h_counts = nullptr;               // pinned
+	unsigned long long *h_state = nullptr;      // pinned
+	int32_t *h_stage = nullptr;                 // pinned, kStageChunks * 4
 	int sms = 0;
 };
 
-namespace {
+namespace hc {
+namespace detail {
+
+
+constexpr uint32_t kStageChunks = 4096; // loads or unloads staged per launch
+constexpr uint32_t kDirtySlack = 65536; // dirty-list room for cells unloaded and loaded again between collects
 
 WorldDev world_dev(const hc_world *w) {
-	return WorldDev{w->desc.nx,  w->desc.ny,  w->desc.nz,   w->desc.cx0, w->desc.cy0,      w->desc.cz0,
-	                w->d_slots,  w->d_dirty,  w->d_hchg,    w->d_flood,  w->pool->d_blocks, w->pool->d_heights};
+	WorldDev W;
+	W.nx = w->desc.nx, W.ny = w->desc.ny, W.nz = w->desc.nz;
+	W.cx0 = w->desc.cx0, W.cy0 = w->desc.cy0, W.cz0 = w->desc.cz0;
+	W.slots = w->d_slots, W.flags = w->d_flags, W.flood = w->d_flood, W.stale = w->d_stale;
+	W.blocks = w->pool->d_blocks, W.heights = w->pool->d_heights, W.pool_cap = w->pool->capacity;
+	W.dirty_list = w->d_dirty_list, W.flood_list = w->d_flood_list, W.hchg_list = w->d_hchg_list;
+	W.stale_list = w->d_stale_list, W.counts = w->d_counts, W.dirty_cap = w->dirty_cap;
+	return W;
 }
 
-} // namespace
+int list_grid(const hc_world *w) { return w->sms * 4; }
+
+// Edits already on the device, then the height recompute they trigger.
+hc_status world_enqueue_edits(hc_world *w, const hc_edit *d_edits, uint32_t n, cudaStream_t st) {
+	hc_ctx *ctx = w->ctx;
+	const WorldDev W = world_dev(w);
+	for (uint32_t first = 0; first < n; first += kEditBatch) {
+		k_apply_edits<<<1, kEditThreads, 0, st>>>(d_edits + first, std::min<uint32_t>(kEditBatch, n - first), W);
+		HC_CUDA(ctx, cudaGetLastError());
+	}
+	return HC_OK;
+}
+
+hc_status world_enqueue_heights(hc_world *w, cudaStream_t st) {
+	hc_ctx *ctx = w->ctx;
+	const WorldDev W = world_dev(w);
+	k_flood_columns<<<list_grid(w), 256, 0, st>>>(W, tables(ctx));
+	HC_CUDA(ctx, cudaGetLastError());
+	k_mark_heights<<<list_grid(w), 256, 0, st>>>(W);
+	HC_CUDA(ctx, cudaGetLastError());
+	return HC_OK;
+}
+
+// Everything of a remesh pass after the edits, reading every length on the device: the remesh list
+// lands in w->d_list (length d_counts[kCountRemesh]).
+hc_status world_enqueue_place(hc_world *w, const int32_t *d_pos, const int32_t *d_slots, uint32_t n, cudaStream_t st) {
+	if (n) {
+		k_place<<<(n + 255) / 256, 256, 0, st>>>(d_pos, d_slots, n, world_dev(w));
+		HC_CUDA(w->ctx, cudaGetLastError());
+	}
+	return HC_OK;
+}
+
+hc_status world_enqueue_evict(hc_world *w, const int32_t *d_pos, uint32_t n, cudaStream_t st) {
+	if (n) {
+		k_evict<<<(n + 255) / 256, 256, 0, st>>>(d_pos, n, world_dev(w));
+		HC_CUDA(w->ctx, cudaGetLastError());
+	}
+	return HC_OK;
+}
+
+Arena world_arena(const hc_world *w, const hc_batch_arena *arena);
+
+hc_status world_enqueue_remesh(hc_world *w, const hc_batch_arena *arena, cudaStream_t st) {
+	hc_ctx *ctx = w->ctx;
+	const WorldDev W = world_dev(w);
+	const Arena A = world_arena(w, arena);
+	k_planes_list<<<w->sms * 8, 256, 0, st>>>(W, tables(ctx), w->pool->d_planes);
+	HC_CUDA(ctx, cudaGetLastError());
+	k_collect<<<1, kEditThreads, kCollectSort * sizeof(uint32_t), st>>>(W, w->d_list, w->d_nbr);
+	HC_CUDA(ctx, cudaGetLastError());
+	HC_CUDA(ctx, cudaMemsetAsync(w->d_state, 0, 4 * sizeof(unsigned long long), st));
+	k_mesh_batch<<<w->sms, kThreads, ctx->smem_bytes, st>>>(
+	    w->pool->d_blocks, w->pool->d_heights, w->pool->d_planes, w->pool->capacity, w->d_nbr, 0u,
+	    w->d_counts + kCountRemesh, reinterpret_cast<unsigned int *>(w->d_state + 2),
+	    reinterpret_cast<unsigned int *>(w->d_state + 3), tables(ctx), A, nullptr, nullptr);
+	HC_CUDA(ctx, cudaGetLastError());
+	k_requeue<<<list_grid(w), 256, 0, st>>>(W, w->d_list, A.results);
+	HC_CUDA(ctx, cudaGetLastError());
+	return HC_OK;
+}
+
+Arena world_arena(const hc_world *w, const hc_batch_arena *arena) {
+	return Arena{reinterpret_cast<uint2 *>(arena->vertices),
+	             arena->indices,
+	             arena->meshes,
+	             w->d_state,
+	             reinterpret_cast<unsigned int *>(w->d_state + 1),
+	             arena->quad_capacity,
+	             arena->mesh_capacity,
+	             arena->results};
+}
+
+hc_status check_arena(hc_ctx *ctx, const hc_batch_arena *arena, uint32_t cells) {
+	if (!arena->vertices || !arena->indices || !arena->meshes || !arena->results)
+		return fail(ctx, HC_ERR_INVALID_ARG, "arena buffers missing");
+	if ((reinterpret_cast<uintptr_t>(arena->vertices) & 15u) || (reinterpret_cast<uintptr_t>(arena->indices) & 3u))
+		return fail(ctx, HC_ERR_INVALID_ARG, "vertices must be 16-byte and indices 4-byte aligned");
+	if (arena->quad_capacity > (1ull << 30))
+		return fail(ctx, HC_ERR_INVALID_ARG, "arena quad capacity above 2^30");
+	(void)cells;
+	return HC_OK;
+}
+
+// Marks every resident slot's planes stale (after the pool was written outside the world's calls).
+hc_status world_touch_all(hc_world *w, const int32_t *slots_host, cudaStream_t st) {
+	hc_ctx *ctx = w->ctx;
+	std::vector<uint8_t> seen(w->pool->capacity, 0);
+	std::vector<int32_t> list;
+	for (int i = 0; i < w->cells; ++i)
+		if (slots_host[i] >= 0 && !seen[slots_host[i]])
+			seen[slots_host[i]] = 1, list.push_back(slots_host[i]);
+	const uint32_t n = (uint32_t)list.size();
+	std::vector<uint32_t> flags(w->pool->capacity, 0);
+	for (int32_t s : list)
+		flags[s] = 1;
+	HC_CUDA(ctx, cudaMemcpyAsync(w->d_stale, flags.data(), flags.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+	if (n)
+		HC_CUDA(ctx, cudaMemcpyAsync(w->d_stale_list, list.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+	HC_CUDA(ctx, cudaMemcpyAsync(w->d_counts + kCountStale, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	return HC_OK;
+}
+
+const uint32_t *world_counts(const hc_world *w) { return w->d_counts; }
+const int32_t *world_remesh_list(const hc_world *w) { return w->d_list; }
+const unsigned long long *world_state(const hc_world *w) { return w->d_state; }
+hc_pool *world_pool(const hc_world *w) { return w->pool; }
+size_t pool_planes_bytes_per_slot() { return kPlaneStride * sizeof(uint32_t); }
+hc_status ctx_fail(hc_ctx *ctx, hc_status s, const std::string &msg) { return fail(ctx, s, msg); }
+int ctx_device(const hc_ctx *ctx) { return ctx->device; }
+
+} // namespace detail
+} // namespace hc
+
+using namespace hc::detail;
 
 extern "C" {
 
@@ -915,9 +1112,11 @@ hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc,
 	HC_CUDA(ctx, cudaSetDevice(ctx->device));
 	hc_world *w = new hc_world();
 	w->ctx = ctx, w->pool = pool, w->desc = *desc, w->cells = (int)cells;
+	w->flood_words = (uint32_t)(desc->nx * desc->nz) * 1024u;
+	w->dirty_cap = (uint32_t)cells + kDirtySlack;
 	cudaDeviceGetAttribute(&w->sms, cudaDevAttrMultiProcessorCount, ctx->device);
-	const size_t cols = (size_t)desc->nx * desc->nz * 1024;
-	cudaError_t e = cudaSuccess;
+	cudaError_t e = cudaFuncSetAttribute(k_collect, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                                     (int)(kCollectSort * sizeof(uint32_t)));
 	const auto A = [&](void **p, size_t bytes) {
 		if (e == cudaSuccess)
 			e = cudaMalloc(p, bytes > 0 ? bytes : 1);
@@ -925,26 +1124,37 @@ hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc,
 			e = cudaMemset(*p, 0, bytes > 0 ? bytes : 1);
 	};
 	A((void **)&w->d_slots, cells * sizeof(int32_t));
-	A((void **)&w->d_dirty, cells);
-	A((void **)&w->d_hchg, cells);
-	A((void **)&w->d_flood, cols * sizeof(uint32_t));
-	A((void **)&w->d_edits, kEditBatch * sizeof(hc_edit));
+	A((void **)&w->d_flags, cells * sizeof(uint32_t));
+	A((void **)&w->d_flood, (size_t)w->flood_words * sizeof(uint32_t));
+	A((void **)&w->d_stale, (size_t)pool->capacity * sizeof(uint32_t));
+	A((void **)&w->d_counts, kCountWords * sizeof(uint32_t));
+	A((void **)&w->d_dirty_list, (size_t)w->dirty_cap * sizeof(int32_t));
+	A((void **)&w->d_flood_list, (size_t)w->flood_words * sizeof(int32_t));
+	A((void **)&w->d_hchg_list, cells * sizeof(int32_t));
+	A((void **)&w->d_stale_list, (size_t)pool->capacity * sizeof(int32_t));
 	A((void **)&w->d_list, cells * sizeof(int32_t));
 	A((void **)&w->d_nbr, cells * 27 * sizeof(int32_t));
-	A((void **)&w->d_slot_mark, pool->capacity);
-	A((void **)&w->d_slot_list, (size_t)pool->capacity * sizeof(int32_t));
-	A((void **)&w->d_count, 2 * sizeof(uint32_t));
+	A((void **)&w->d_edits, kEditBatch * sizeof(hc_edit));
+	A((void **)&w->d_stage, kStageChunks * 4 * sizeof(int32_t));
 	A((void **)&w->d_state, 4 * sizeof(unsigned long long));
 	if (e == cudaSuccess)
-		e = cudaMallocHost(&w->h_count, 2 * sizeof(uint32_t));
+		e = cudaMallocHost(&w->h_counts, kCountWords * sizeof(uint32_t));
 	if (e == cudaSuccess)
 		e = cudaMallocHost(&w->h_state, 4 * sizeof(unsigned long long));
+	if (e == cudaSuccess)
+		e = cudaMallocHost(&w->h_stage, kStageChunks * 4 * sizeof(int32_t));
 	if (e == cudaSuccess)
 		e = cudaMemcpy(w->d_slots, slots, cells * sizeof(int32_t), cudaMemcpyHostToDevice);
 	if (e != cudaSuccess) {
 		hc_world_destroy(w);
 		return fail(ctx, e == cudaErrorMemoryAllocation ? HC_ERR_OUT_OF_MEMORY : HC_ERR_CUDA,
 		            std::string("world: ") + cudaGetErrorString(e));
+	}
+	// every resident chunk's planes are built before the first remesh
+	const hc_status s = world_touch_all(w, slots, ctx->stream);
+	if (s != HC_OK) {
+		hc_world_destroy(w);
+		return s;
 	}
 	*out = w;
 	return HC_OK;
@@ -954,19 +1164,13 @@ void hc_world_destroy(hc_world *w) {
 	if (!w)
 		return;
 	cudaSetDevice(w->ctx->device);
-	cudaFree(w->d_slots);
-	cudaFree(w->d_dirty);
-	cudaFree(w->d_hchg);
-	cudaFree(w->d_flood);
-	cudaFree(w->d_edits);
-	cudaFree(w->d_list);
-	cudaFree(w->d_nbr);
-	cudaFree(w->d_slot_mark);
-	cudaFree(w->d_slot_list);
-	cudaFree(w->d_count);
-	cudaFree(w->d_state);
-	cudaFreeHost(w->h_count);
+	for (void *p : {(void *)w->d_slots, (void *)w->d_flags, (void *)w->d_flood, (void *)w->d_stale, (void *)w->d_counts,
+	                (void *)w->d_dirty_list, (void *)w->d_flood_list, (void *)w->d_hchg_list, (void *)w->d_stale_list,
+	                (void *)w->d_list, (void *)w->d_nbr, (void *)w->d_edits, (void *)w->d_stage, (void *)w->d_state})
+		cudaFree(p);
+	cudaFreeHost(w->h_counts);
 	cudaFreeHost(w->h_state);
+	cudaFreeHost(w->h_stage);
 	delete w;
 }
 
@@ -976,82 +1180,111 @@ hc_status hc_world_apply_edits(hc_world *w, const hc_edit *edits, uint32_t n, in
 	hc_ctx *ctx = w->ctx;
 	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
 	HC_CUDA(ctx, cudaSetDevice(ctx->device));
-	const WorldDev W = world_dev(w);
-	for (uint32_t first = 0; first < n; first += kEditBatch) {
-		const uint32_t nb = std::min<uint32_t>(kEditBatch, n - first);
-		const hc_edit *src = edits + first;
-		if (!src_on_device) {
-			HC_CUDA(ctx, cudaMemcpyAsync(w->d_edits, src, nb * sizeof(hc_edit), cudaMemcpyHostToDevice, st));
-			src = w->d_edits;
-		}
-		k_apply_edits<<<1, kEditThreads, 0, st>>>(src, nb, W);
-		HC_CUDA(ctx, cudaGetLastError());
-		if (!src_on_device)
+	hc_status s;
+	if (src_on_device) {
+		if ((s = world_enqueue_edits(w, edits, n, st)) != HC_OK)
+			return s;
+	} else {
+		for (uint32_t first = 0; first < n; first += kEditBatch) {
+			const uint32_t nb = std::min<uint32_t>(kEditBatch, n - first);
+			HC_CUDA(ctx, cudaMemcpyAsync(w->d_edits, edits + first, nb * sizeof(hc_edit), cudaMemcpyHostToDevice, st));
+			if ((s = world_enqueue_edits(w, w->d_edits, nb, st)) != HC_OK)
+				return s;
 			HC_CUDA(ctx, cudaStreamSynchronize(st)); // d_edits is reused by the next batch
+		}
 	}
-	const uint32_t cols = (uint32_t)(w->desc.nx * w->desc.nz) * 1024u;
-	k_flood_columns<<<(cols + 255) / 256, 256, 0, st>>>(W, tables(ctx));
-	HC_CUDA(ctx, cudaGetLastError());
-	k_mark_heights<<<(w->cells + 255) / 256, 256, 0, st>>>(W);
-	HC_CUDA(ctx, cudaGetLastError());
+	return world_enqueue_heights(w, st);
+}
+
+hc_status hc_world_load(hc_world *w, const hc_chunk_load *loads, uint32_t n, void *stream) {
+	if (!w || (!loads && n))
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = w->ctx;
+	for (uint32_t i = 0; i < n; ++i)
+		if (loads[i].slot < 0 || (uint32_t)loads[i].slot >= w->pool->capacity || !loads[i].blocks || !loads[i].heights)
+			return fail(ctx, HC_ERR_INVALID_ARG, "load: slot beyond the pool or data missing");
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	for (uint32_t first = 0; first < n; first += kStageChunks) {
+		const uint32_t nb = std::min<uint32_t>(kStageChunks, n - first);
+		for (uint32_t i = 0; i < nb; ++i) {
+			const hc_chunk_load &l = loads[first + i];
+			HC_CUDA(ctx, cudaMemcpyAsync(w->pool->d_blocks + (size_t)l.slot * 32768, l.blocks, 32768 * sizeof(uint16_t),
+			                             cudaMemcpyHostToDevice, st));
+			HC_CUDA(ctx, cudaMemcpyAsync(w->pool->d_heights + (size_t)l.slot * 1024, l.heights, 1024,
+			                             cudaMemcpyHostToDevice, st));
+			w->h_stage[3 * i] = l.cx, w->h_stage[3 * i + 1] = l.cy, w->h_stage[3 * i + 2] = l.cz;
+			w->h_stage[3 * nb + i] = l.slot;
+		}
+		HC_CUDA(ctx, cudaMemcpyAsync(w->d_stage, w->h_stage, 4 * nb * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+		const hc_status s = world_enqueue_place(w, w->d_stage, w->d_stage + 3 * nb, nb, st);
+		if (s != HC_OK)
+			return s;
+		HC_CUDA(ctx, cudaStreamSynchronize(st)); // the staging buffers are reused
+	}
 	return HC_OK;
+}
+
+hc_status hc_world_unload(hc_world *w, const int32_t *positions, uint32_t n, void *stream) {
+	if (!w || (!positions && n))
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = w->ctx;
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	for (uint32_t first = 0; first < n; first += kStageChunks) {
+		const uint32_t nb = std::min<uint32_t>(kStageChunks, n - first);
+		std::memcpy(w->h_stage, positions + 3 * (size_t)first, 3 * nb * sizeof(int32_t));
+		HC_CUDA(ctx, cudaMemcpyAsync(w->d_stage, w->h_stage, 3 * nb * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+		const hc_status s = world_enqueue_evict(w, w->d_stage, nb, st);
+		if (s != HC_OK)
+			return s;
+		HC_CUDA(ctx, cudaStreamSynchronize(st));
+	}
+	return HC_OK;
+}
+
+hc_status hc_world_touch(hc_world *w, void *stream) {
+	if (!w)
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = w->ctx;
+	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	std::vector<int32_t> slots(w->cells);
+	HC_CUDA(ctx, cudaMemcpyAsync(slots.data(), w->d_slots, w->cells * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	return world_touch_all(w, slots.data(), st);
 }
 
 hc_status hc_world_remesh(hc_world *w, const hc_batch_arena *arena, int32_t *cells, uint32_t cap, uint32_t *n_remeshed,
                           uint64_t *quads, uint32_t *meshes, void *stream) {
-	if (!w || !arena || !n_remeshed || !arena->vertices || !arena->indices || !arena->meshes || !arena->results)
+	if (!w || !arena || !n_remeshed || (!cells && cap))
 		return HC_ERR_INVALID_ARG;
 	hc_ctx *ctx = w->ctx;
-	if ((reinterpret_cast<uintptr_t>(arena->vertices) & 15u) || (reinterpret_cast<uintptr_t>(arena->indices) & 3u))
-		return fail(ctx, HC_ERR_INVALID_ARG, "vertices must be 16-byte and indices 4-byte aligned");
+	hc_status s = check_arena(ctx, arena, (uint32_t)w->cells);
+	if (s != HC_OK)
+		return s;
+	if (cap < (uint32_t)w->cells)
+		return fail(ctx, HC_ERR_INVALID_ARG, "cells must hold one entry per grid cell");
 	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
 	HC_CUDA(ctx, cudaSetDevice(ctx->device));
-	const WorldDev W = world_dev(w);
-	k_collect<<<1, kEditThreads, 0, st>>>(W, w->d_list, w->d_nbr, w->d_slot_mark, w->pool->capacity, w->d_slot_list,
-	                                      w->d_count);
-	HC_CUDA(ctx, cudaGetLastError());
-	HC_CUDA(ctx, cudaMemcpyAsync(w->h_count, w->d_count, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-	HC_CUDA(ctx, cudaStreamSynchronize(st));
-	const uint32_t n = w->h_count[0], ns = w->h_count[1];
-	*n_remeshed = n;
-	if (quads)
-		*quads = 0;
-	if (meshes)
-		*meshes = 0;
-	if (n == 0)
-		return HC_OK;
-	const auto remark = [&](const char *msg) {
-		k_remark<<<(n + 255) / 256, 256, 0, st>>>(W, w->d_list, n);
-		cudaStreamSynchronize(st);
-		return fail(ctx, HC_ERR_CAPACITY, msg);
-	};
-	if (n > cap || !cells)
-		return remark("cells buffer too small for the chunks to remesh");
-	HC_CUDA(ctx, cudaMemsetAsync(w->d_state, 0, 4 * sizeof(unsigned long long), st));
-	k_planes_pool<<<(int)std::min<uint64_t>(((uint64_t)ns * kPlaneWords + 255) / 256, (uint64_t)w->sms * 8), 256, 0, st>>>(
-	    w->pool->d_blocks, w->pool->d_heights, w->d_slot_list, ns, tables(ctx), w->pool->d_planes);
-	HC_CUDA(ctx, cudaGetLastError());
-	const Arena A{reinterpret_cast<uint2 *>(arena->vertices),
-	              arena->indices,
-	              arena->meshes,
-	              w->d_state,
-	              reinterpret_cast<unsigned int *>(w->d_state + 1),
-	              arena->quad_capacity,
-	              arena->mesh_capacity,
-	              arena->results};
-	k_mesh_batch<<<w->sms, kThreads, ctx->smem_bytes, st>>>(
-	    w->pool->d_blocks, w->pool->d_heights, w->pool->d_planes, w->pool->capacity, w->d_nbr, n,
-	    reinterpret_cast<unsigned int *>(w->d_state + 2), reinterpret_cast<unsigned int *>(w->d_state + 3), tables(ctx), A);
-	HC_CUDA(ctx, cudaGetLastError());
+	if ((s = world_enqueue_remesh(w, arena, st)) != HC_OK)
+		return s;
+	HC_CUDA(ctx, cudaMemcpyAsync(w->h_counts, w->d_counts, kCountWords * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
 	HC_CUDA(ctx, cudaMemcpyAsync(w->h_state, w->d_state, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-	HC_CUDA(ctx, cudaMemcpyAsync(cells, w->d_list, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
 	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	const uint32_t n = w->h_counts[kCountRemesh];
+	*n_remeshed = n;
+	if (n) {
+		HC_CUDA(ctx, cudaMemcpyAsync(cells, w->d_list, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+		HC_CUDA(ctx, cudaStreamSynchronize(st));
+	}
 	if (quads)
-		*quads = w->h_state[0];
+		*quads = std::min<unsigned long long>(w->h_state[0], arena->quad_capacity);
 	if (meshes)
-		*meshes = (uint32_t)(w->h_state[1] & 0xffffffffu);
-	if (w->h_state[0] > arena->quad_capacity || (w->h_state[1] & 0xffffffffu) > arena->mesh_capacity)
-		return remark("arena too small for the remeshed chunks");
+		*meshes = std::min<uint32_t>((uint32_t)(w->h_state[1] & 0xffffffffu), arena->mesh_capacity);
+	if (w->h_state[3])
+		return fail(ctx, HC_ERR_CAPACITY, std::to_string(w->h_state[3]) +
+		                                      " chunks did not fit the arena; they stay marked for the next remesh");
 	return HC_OK;
 }
 
@@ -1260,7 +1493,8 @@ extern "C" hc_status hc_mesh_batch_noalloc(const uint16_t *pool_blocks, const in
 		        mesh_capacity,
 		        results};
 		k_mesh_batch<<<D.sms, kThreads, sizeof(Smem), st>>>(pool_blocks, pool_heights, nullptr, pool_capacity, neighbours,
-		                                                     n, state + 4, state + 5, DevTables{D.class_of, D.classes}, A);
+		                                                     n, nullptr, state + 4, state + 5, DevTables{D.class_of, D.classes}, A,
+		                                                     nullptr, nullptr);
 		e = cudaGetLastError();
 	}
 	uint32_t host_state[kNoAllocStateWords];

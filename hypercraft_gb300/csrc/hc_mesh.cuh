@@ -695,7 +695,10 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		uint32_t co, ct, to, tt;
 		custom_count(S, tid * kBlocksPerThread, co, ct);
 		block_scan2(S, co, ct, eo, et, to, tt);
-		relight_window(S, T); // the relight scratch shares memory with the plane masks
+		if (S.lgt[26])
+			light_from_batch(S);
+		else
+			relight_window(S, T); // the relight scratch shares memory with the plane masks
 		__syncthreads();
 		plane_visibility(S);
 		__syncthreads();

@@ -279,4 +279,160 @@ __device__ __forceinline__ bool chunk_plane_row(const uint16_t *blk, const int8_
 	return low;
 }
 
+// Bit planes of chunks: one thread per 32-cell row, 32 rows (one flag word) per warp.
+__device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hgt, const DevClass *cls_smem,
+                                           const uint8_t *class_of, int r, uint32_t *out) {
+	uint32_t pass, sun, t15;
+	const bool low = chunk_plane_row(blk, hgt, cls_smem, class_of, r >> 5, r & 31, pass, sun, t15);
+	out[kPlanePass * kPlaneWords + r] = pass;
+	out[kPlaneSun * kPlaneWords + r] = sun;
+	out[kPlaneT15 * kPlaneWords + r] = t15;
+	const uint32_t lows = __ballot_sync(0xffffffffu, low);
+	if ((threadIdx.x & 31) == 0)
+		out[3 * kPlaneWords + (r >> 5)] = lows;
+}
+
+
+// ------------------------------------------------------------------------------- batch light pass
+//
+// The batched form lights all chunks of a batch at once instead of relighting a 62^3 window per
+// chunk (which covers each cell about seven times). On the box [-1, 33)^3 of a chunk the window's
+// fixpoint equals the fixpoint of the same rule over every chunk of the batch without the window
+// and border bounds: a light path that ends in the box at level >= 1 only visits cells whose level
+// exceeds their distance to the box, and level <= 15 keeps such cells inside [-15, 47)^3, which
+// lies inside the 27 chunks the batch holds for that chunk. So with S_t = {cells of level >= t}
+// over the batch,
+//     S_15 = seeds of level 15,   S_t = S_{t+1} | seeds of level t | (pass & dilate6(S_{t+1})),
+// fifteen passes over all chunks give every level; face neighbours missing from the batch count as
+// dark (they lie outside every meshed chunk's window).
+
+constexpr int kLevels = 15;
+constexpr size_t kLevelSlotWords = (size_t)2 * kLevels * kPlaneWords; // per chunk: 2 channels x 15 levels
+
+struct LightPass {
+	const int32_t *slots;   // batch chunk -> pool slot
+	const int32_t *nb6;     // batch chunk -> face neighbours (batch chunk or -1): -x, +x, -y, +y, -z, +z
+	const uint32_t *planes; // pool planes (pass, sun, level-15 emitters, low-emitter rows)
+	const uint16_t *blocks; // pool blocks (rows with emitters below 15)
+	uint32_t *levels;       // batch chunk -> channel -> level t at plane t - 1 -> 1024 rows
+	uint8_t *light;         // batch chunk -> 32768 cells (sun | torch << 4), the reference's cell order
+	uint32_t n;             // batch chunks
+};
+
+__device__ __forceinline__ const uint32_t *level_plane(const LightPass &L, int i, int c, int t) {
+	return L.levels + (size_t)i * kLevelSlotWords + (size_t)(c * kLevels + t - 1) * kPlaneWords;
+}
+
+__device__ __forceinline__ uint32_t mux(uint32_t c, uint32_t a, uint32_t b) { return (c & a) | (~c & b); }
+
+// 4-bit light of the 32 cells of a row from its 15 nested level words (s[t - 1] = S_t).
+__device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
+	b[3] = s[7];
+	b[2] = mux(b[3], s[11], s[3]);
+	b[1] = mux(b[3], mux(b[2], s[13], s[9]), mux(b[2], s[5], s[1]));
+	b[0] = mux(b[3], mux(b[2], mux(b[1], s[14], s[12]), mux(b[1], s[10], s[8])),
+	           mux(b[2], mux(b[1], s[6], s[4]), mux(b[1], s[2], s[0])));
+}
+
+// Level t of every row of every batch chunk (one thread per row, both channels); level 1 also
+// writes the cells' light bytes.
+__global__ void __launch_bounds__(256) k_light_level(LightPass L, DevTables T, int t) {
+	const uint64_t total = (uint64_t)L.n * kPlaneWords;
+	for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x) {
+		const int i = (int)(g >> 10), r = (int)(g & 1023u), y = r >> 5, z = r & 31;
+		const uint32_t *P = L.planes + (size_t)L.slots[i] * kPlaneStride;
+		uint32_t s[2];
+		if (t == kLevels) {
+			s[0] = __ldg(P + kPlaneSun * kPlaneWords + r);
+			s[1] = __ldg(P + kPlaneT15 * kPlaneWords + r);
+		} else {
+			const int *nb = L.nb6 + 6 * i;
+			const int xm = nb[0], xp = nb[1];
+			const int yi = y > 0 ? i : nb[2], yr = y > 0 ? r - 32 : r + 31 * 32;
+			const int yj = y < 31 ? i : nb[3], yq = y < 31 ? r + 32 : r - 31 * 32;
+			const int zi = z > 0 ? i : nb[4], zr = z > 0 ? r - 1 : r + 31;
+			const int zj = z < 31 ? i : nb[5], zq = z < 31 ? r + 1 : r - 31;
+			const uint32_t pass = __ldg(P + kPlanePass * kPlaneWords + r);
+#pragma unroll
+			for (int c = 0; c < 2; ++c) {
+				const uint32_t prev = level_plane(L, i, c, t + 1)[r];
+				uint32_t d = (prev << 1) | (prev >> 1);
+				if (xm >= 0)
+					d |= level_plane(L, xm, c, t + 1)[r] >> 31;
+				if (xp >= 0)
+					d |= level_plane(L, xp, c, t + 1)[r] << 31;
+				if (yi >= 0)
+					d |= level_plane(L, yi, c, t + 1)[yr];
+				if (yj >= 0)
+					d |= level_plane(L, yj, c, t + 1)[yq];
+				if (zi >= 0)
+					d |= level_plane(L, zi, c, t + 1)[zr];
+				if (zj >= 0)
+					d |= level_plane(L, zj, c, t + 1)[zq];
+				s[c] = prev | (pass & d);
+			}
+		}
+		if ((__ldg(P + 3 * kPlaneWords + (r >> 5)) >> (r & 31)) & 1u) { // emitters below level 15 in this row
+			const uint16_t *row = L.blocks + (size_t)L.slots[i] * 32768 + r * 32;
+			for (int x = 0; x < 32; ++x)
+				if (T.classes[T.class_of[row[x]]].light >= t)
+					s[1] |= 1u << x;
+		}
+		uint32_t *out0 = L.levels + (size_t)i * kLevelSlotWords + (size_t)(t - 1) * kPlaneWords + r;
+		out0[0] = s[0];
+		out0[(size_t)kLevels * kPlaneWords] = s[1];
+		if (t == 1) {
+			uint32_t lv[kLevels], b[2][4];
+#pragma unroll
+			for (int c = 0; c < 2; ++c) {
+				lv[0] = s[c];
+#pragma unroll
+				for (int u = 2; u <= kLevels; ++u)
+					lv[u - 1] = level_plane(L, i, c, u)[r];
+				level_bits(lv, b[c]);
+			}
+			uint32_t w[8];
+#pragma unroll
+			for (int q = 0; q < 8; ++q) {
+				uint32_t v = 0;
+#pragma unroll
+				for (int k = 0; k < 4; ++k) {
+					const int x = 4 * q + k;
+					uint32_t byte = 0;
+#pragma unroll
+					for (int bit = 0; bit < 4; ++bit)
+						byte |= ((b[0][bit] >> x) & 1u) << bit | ((b[1][bit] >> x) & 1u) << (bit + 4);
+					v |= byte << (8 * k);
+				}
+				w[q] = v;
+			}
+			uint4 *dst = reinterpret_cast<uint4 *>(L.light + (size_t)i * 32768 + r * 32);
+			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+		}
+	}
+}
+
+// Light of [-1, 32]^3 from the batch light pass (instead of relight_window): the chunk's own rows
+// and the neighbours' edge cells, into the low byte of every staged cell.
+__device__ void light_from_batch(Smem &S) {
+	uint8_t *light = light_bytes(S);
+	for (int k = threadIdx.x; k < kLt * kLt * 10; k += kThreads) {
+		const int row = k / 10, part = k - row * 10;
+		const int y = row / kLt - 1, z = row % kLt - 1;
+		uint8_t *dst = light + 2 * (row * kLt + 1); // cell x = 0 of the row
+		const int in = ((y & 31) * 32 + (z & 31)) * 32;
+		if (part < 8) {
+			const uint32_t v = *reinterpret_cast<const uint32_t *>(S.lgt[nb_index(0, y, z)] + in + 4 * part);
+#pragma unroll
+			for (int b = 0; b < 4; ++b)
+				dst[2 * (4 * part + b)] = (uint8_t)(v >> (8 * b));
+		} else if (part == 8) {
+			dst[-2] = S.lgt[nb_index(-1, y, z)][in + 31];
+		} else {
+			dst[2 * 32] = S.lgt[nb_index(32, y, z)][in];
+		}
+	}
+}
+
 } // namespace hc

@@ -20,6 +20,11 @@ class _Desc(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in ("nx", "ny", "nz", "cx0", "cy0", "cz0")]
 
 
+class ChunkLoad(ctypes.Structure):
+    _fields_ = [("cx", ctypes.c_int32), ("cy", ctypes.c_int32), ("cz", ctypes.c_int32), ("slot", ctypes.c_int32),
+                ("blocks", ctypes.c_void_p), ("heights", ctypes.c_void_p)]
+
+
 def _bind(lib):
     if getattr(lib, "_world_bound", False):
         return lib
@@ -30,6 +35,9 @@ def _bind(lib):
     lib.hc_world_apply_edits.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_int, vp]
     lib.hc_world_remesh.argtypes = [vp, P(batch._Arena), vp, ctypes.c_uint32, P(ctypes.c_uint32),
                                     P(ctypes.c_uint64), P(ctypes.c_uint32), vp]
+    lib.hc_world_load.argtypes = [vp, P(ChunkLoad), ctypes.c_uint32, vp]
+    lib.hc_world_unload.argtypes = [vp, vp, ctypes.c_uint32, vp]
+    lib.hc_world_touch.argtypes = [vp, vp]
     lib._world_bound = True
     return lib
 
@@ -37,12 +45,16 @@ def _bind(lib):
 class ResidentWorld:
     """A generated world (worldgen.World) resident in a device pool, slot = chunk index."""
 
-    def __init__(self, ctx: Context, world):
+    def __init__(self, ctx: Context, world, resident=None, capacity=None):
+        """resident: optional bool mask of the chunks loaded at creation (default all); chunk i
+        uses pool slot i."""
         self.ctx, self.world = ctx, world
         self.lib = _bind(batch._bind(library()))
-        self.pool = batch.Pool(ctx, world.n_chunks)
+        self.pool = batch.Pool(ctx, capacity or world.n_chunks)
         self.pool.upload(0, world.blocks, world.heights)
         slots = np.arange(world.n_chunks, dtype=np.int32)
+        if resident is not None:
+            slots[~np.asarray(resident, bool)] = -1
         h = ctypes.c_void_p()
         desc = _Desc(world.nx, world.ny, world.nz, *world.origin)
         ctx.check(self.lib.hc_world_create(ctx.handle, self.pool.handle, ctypes.byref(desc), slots.ctypes.data,
@@ -59,15 +71,45 @@ class ResidentWorld:
             self.ctx.check(self.lib.hc_world_apply_edits(self.handle, e.ctypes.data, len(e), 0, stream),
                            "hc_world_apply_edits")
 
-    def remesh(self, arena: batch.Arena, stream=None):
-        """Relights + meshes the marked chunks into arena; returns (cells, quads, meshes)."""
+    def load(self, cells, blocks=None, heights=None, stream=None):
+        """Loads grid cells (chunk i into pool slot i) from the world's arrays, or from the given
+        (n, 32768) blocks and (n, 1024) heights."""
+        cells = np.asarray(cells, np.int64)
+        b = np.ascontiguousarray(self.world.blocks[cells] if blocks is None else blocks, np.uint16)
+        h = np.ascontiguousarray(self.world.heights[cells] if heights is None else heights, np.int8)
+        loads = (ChunkLoad * len(cells))()
+        for i, c in enumerate(cells):
+            ix, iy, iz = self.world.coords(int(c))
+            ox, oy, oz = self.world.origin
+            loads[i] = ChunkLoad(ox + ix, oy + iy, oz + iz, int(c), b[i].ctypes.data, h[i].ctypes.data)
+        self.ctx.check(self.lib.hc_world_load(self.handle, loads, len(cells), stream), "hc_world_load")
+
+    def unload(self, cells, stream=None):
+        pos = np.array([[o + c for o, c in zip(self.world.origin, self.world.coords(int(i)))] for i in cells],
+                       np.int32).reshape(-1, 3)
+        self.ctx.check(self.lib.hc_world_unload(self.handle, pos.ctypes.data, len(pos), stream), "hc_world_unload")
+
+    def touch(self, stream=None):
+        """Rebuilds every resident chunk's light planes (after writing the pool directly)."""
+        self.ctx.check(self.lib.hc_world_touch(self.handle, stream), "hc_world_touch")
+
+    def remesh(self, arena: batch.Arena, stream=None, partial: bool = False):
+        """Relights + meshes the marked chunks into arena; returns (cells, quads, meshes). With
+        partial=True a full arena is not an error: returns (cells, quads, meshes, status) where
+        status[i] != 0 marks a chunk that did not fit (it stays marked for the next call)."""
+        from .mesher import HcError, HC_ERR_CAPACITY
         cells = np.empty(self.world.n_chunks, np.int32)
         n, q, m = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint32()
         a = arena.c()
-        self.ctx.check(self.lib.hc_world_remesh(self.handle, ctypes.byref(a), cells.ctypes.data, len(cells),
-                                                ctypes.byref(n), ctypes.byref(q), ctypes.byref(m), stream),
-                       "hc_world_remesh")
-        return cells[:n.value].copy(), q.value, m.value
+        st = self.lib.hc_world_remesh(self.handle, ctypes.byref(a), cells.ctypes.data, len(cells), ctypes.byref(n),
+                                      ctypes.byref(q), ctypes.byref(m), stream)
+        if not (partial and st == HC_ERR_CAPACITY):
+            self.ctx.check(st, "hc_world_remesh")
+        cells = cells[:n.value].copy()
+        if not partial:
+            return cells, q.value, m.value
+        status = arena.results_host(len(cells))[:, 4].copy()
+        return cells, q.value, m.value, status
 
     def download(self):
         return batch.pool_download(self.pool, 0, self.world.n_chunks)

@@ -184,7 +184,9 @@ typedef struct hc_edit {
 } hc_edit;
 
 /* Grid cell (ix, iy, iz), index ix + nx * (iz + nz * iy), holds chunk (cx0 + ix, cy0 + iy, cz0 + iz)
- * in pool slot slots[index] (host array), or -1 when that chunk is not resident. */
+ * in pool slot slots[index] (host array), or -1 when that chunk is not resident. A resident
+ * chunk's blocks and heights change only through the hc_world_* calls below, or the caller says
+ * so with hc_world_touch. Calls on one world are ordered on the stream they name. */
 hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc, const int32_t *slots, hc_world **out);
 void hc_world_destroy(hc_world *world);
 
@@ -197,12 +199,124 @@ void hc_world_destroy(hc_world *world);
  * every chunk whose heights changed. `edits` is a host or device array (src_on_device). */
 hc_status hc_world_apply_edits(hc_world *world, const hc_edit *edits, uint32_t n, int src_on_device, void *stream);
 
+/* A chunk entering the world (replaces ChunkTaskRunner<kGenerate>::Run,
+ * client/src/ChunkGenerateTask.cpp:22-42): its blocks (32768 uint16) and sunlight heights
+ * (1024 int8), host memory, are copied into pool slot `slot`, and it is marked for remeshing. */
+typedef struct hc_chunk_load {
+	int32_t cx, cy, cz; /* chunk position */
+	int32_t slot;       /* free pool slot */
+	const uint16_t *blocks;
+	const int8_t *heights;
+} hc_chunk_load;
+
+/* Loads `n` chunks (positions outside the grid are skipped). Each is marked for remeshing, and so
+ * is every marked neighbour that waited for it. Returns once the host data has been copied. */
+hc_status hc_world_load(hc_world *world, const hc_chunk_load *loads, uint32_t n, void *stream);
+/* Takes `n` chunks (positions: host int32 x 3n) out of the world; their slots are free once the
+ * stream passes this point. A pending remesh of them is dropped (ChunkTaskData<kMesh>::OnUnload). */
+hc_status hc_world_unload(hc_world *world, const int32_t *positions, uint32_t n, void *stream);
+/* Rebuilds the per-chunk light planes of every resident chunk before the next remesh: call after
+ * writing resident chunks' pool data by other means (hc_pool_upload). Synchronous. */
+hc_status hc_world_touch(hc_world *world, void *stream);
+
 /* Relights and meshes every marked chunk whose 26 neighbours are resident (the reference's kMesh
- * waits for them too), in grid order, into `arena` (chunk i of the batch = cells[i]); clears their
- * marks. cells (host, capacity cap) receives the grid indices; *n_remeshed their number. On
- * HC_ERR_CAPACITY nothing is cleared and *n_remeshed holds the number of chunks waiting. */
+ * waits for them too), in grid order, into `arena` (chunk i of the batch = cells[i]; arena
+ * results hold one entry per grid cell); clears their marks. A marked chunk with a missing
+ * neighbour waits until a neighbour is loaded. cells (host, cap >= grid cells) receives the grid
+ * indices; *n_remeshed their number. A chunk that does not fit the arena reports status 1 in its
+ * result words, stays marked for the next remesh, and the call returns HC_ERR_CAPACITY. */
 hc_status hc_world_remesh(hc_world *world, const hc_batch_arena *arena, int32_t *cells, uint32_t cap,
                           uint32_t *n_remeshed, uint64_t *quads, uint32_t *meshes, void *stream);
+
+/* ----------------------------------------------------------------------------------------------
+ * Request server: continuous batching of world requests into fixed ticks.
+ *
+ * Replaces the reference's chunk task scheduling: ChunkTaskPool (client/src/ChunkTaskPool.cpp:
+ * 16-130) with its worker threads (client/src/WorldWorker.cpp:18-27) and LocalClient's chunk loader
+ * (client/src/LocalClient.cpp:14-27). Requests arrive at any time (hc_server_submit); every tick
+ * the server admits, in arrival order, the requests that fit the tick (edits, with a fill counted
+ * as its voxels, up to max_edits_per_tick; loads and unloads up to max_loads_per_tick; a load
+ * needs a free pool slot, and slots freed by unloads return once their tick completes) and runs
+ * one device pass for them: unloads, loads, edits, sunlight heights, then relight + remesh of every
+ * chunk they marked (as hc_world_*). Up to `depth` passes are in flight; each has its own arena.
+ * A load or unload of a chunk that an earlier request of the same tick edits waits for the next
+ * tick, so the result equals applying the requests one at a time in arrival order.
+ * ---------------------------------------------------------------------------------------------- */
+typedef struct hc_server hc_server;
+
+typedef struct hc_server_config {
+	uint32_t tick_us;            /* tick period in microseconds */
+	uint32_t depth;              /* passes in flight, 1..8 */
+	uint32_t max_edits_per_tick; /* edits per tick, a fill counting as its voxels */
+	uint32_t max_loads_per_tick; /* loads + unloads per tick */
+	uint64_t arena_quads;        /* per pass in flight; a chunk that does not fit is remeshed by a later pass */
+	uint32_t arena_meshes;
+	uint32_t reserved;
+} hc_server_config;
+
+enum { HC_REQ_EDIT = 0, HC_REQ_FILL = 1, HC_REQ_LOAD = 2, HC_REQ_UNLOAD = 3 };
+
+typedef struct hc_request {
+	uint32_t kind;          /* HC_REQ_* */
+	uint32_t block;         /* EDIT, FILL: new raw block */
+	int32_t x, y, z;        /* EDIT: voxel; FILL: lowest corner voxel; LOAD, UNLOAD: chunk position */
+	uint32_t size;          /* FILL: edge length in voxels, 1..32 */
+	const uint16_t *blocks; /* LOAD: 32768 blocks (host), read when the request is admitted */
+	const int8_t *heights;  /* LOAD: 1024 sunlight heights (host) */
+	uint64_t tag;           /* echoed in the completion */
+} hc_request;
+
+typedef struct hc_completion {
+	uint64_t tag;
+	uint32_t kind;
+	uint32_t status; /* 0 done; 1 rejected (position outside the grid, bad fill size, missing data) */
+	uint64_t tick;
+	uint64_t submit_ns, done_ns; /* steady clock: submitted, and its pass observed complete */
+} hc_completion;
+
+typedef struct hc_server_stats {
+	uint64_t ticks, requests_done, requests_rejected;
+	uint64_t chunks_remeshed, chunks_requeued, quads;
+	uint64_t edits, loads, unloads;
+	uint64_t gpu_ns_total, gpu_ns_max; /* device time of the passes */
+	uint32_t pool_capacity, resident, free_slots, queued;
+} hc_server_stats;
+
+/* Called on the server's completion thread after each pass, with host copies of its output: the
+ * remeshed grid cells, their result words (5 each), and the arena's vertices, indices and mesh
+ * descriptors (offsets as in hc_batch_arena). For tests and tools: it costs a full read-back. */
+typedef void (*hc_tick_sink)(void *user, uint64_t tick, uint32_t n_chunks, const int32_t *cells,
+                             const uint32_t *results, const uint32_t *vertices, const uint16_t *indices,
+                             const hc_mesh_desc *meshes, uint64_t quads, uint32_t mesh_count);
+
+/* Creates a server over an empty world grid with a chunk pool of `pool_capacity` slots (0: as many
+ * as free device memory allows, keeping 2 GiB, at most 65536). */
+hc_status hc_server_create(hc_ctx *ctx, const hc_world_desc *desc, uint32_t pool_capacity,
+                           const hc_server_config *config, hc_server **out);
+/* Stops the server (as hc_server_stop) and frees it. */
+void hc_server_destroy(hc_server *server);
+/* Queues requests (thread-safe). */
+hc_status hc_server_submit(hc_server *server, const hc_request *requests, uint32_t n);
+/* Starts the tick and completion threads. */
+hc_status hc_server_start(hc_server *server);
+/* Waits until every submitted request has completed and no chunk is left marked, then stops. */
+hc_status hc_server_stop(hc_server *server);
+/* Without the threads: admits what fits one tick, runs its pass and waits for it. */
+hc_status hc_server_step(hc_server *server, uint32_t *admitted);
+/* Takes up to `cap` completions, oldest first. */
+hc_status hc_server_poll(hc_server *server, hc_completion *out, uint32_t cap, uint32_t *n);
+hc_status hc_server_get_stats(hc_server *server, hc_server_stats *out);
+/* Sets the per-pass sink (NULL: none); only while stopped. */
+hc_status hc_server_set_sink(hc_server *server, hc_tick_sink sink, void *user);
+/* The pool slot of every grid cell (-1: not resident) as of the last admitted tick. */
+hc_status hc_server_resident(hc_server *server, int32_t *cell_slots);
+/* The server's chunk pool (for hc_pool_download while it is idle). */
+hc_pool *hc_server_pool(hc_server *server);
+/* Replays a timed request trace on a started server: request i is submitted arrival_ns[i] after
+ * the call starts (its tag becomes i); returns once all have completed, with latency_ns[i] from
+ * its arrival time to its completion and *elapsed_ns from the start to the last completion. */
+hc_status hc_server_replay(hc_server *server, const hc_request *requests, const uint64_t *arrival_ns, uint32_t n,
+                           uint64_t *latency_ns, uint64_t *elapsed_ns);
 
 /* ----------------------------------------------------------------------------------------------
  * Batched meshing that allocates nothing. No counterpart in the reference.

@@ -75,3 +75,79 @@ def test_edits_outside_the_world_are_ignored(ctx, oracle):
     far = e.copy()
     far["y"] += 10_000
     _run(ctx, oracle, np.concatenate([e, far]), hw.edit_world)
+
+
+def test_loads_wait_for_neighbours_and_unloads_drop(ctx, oracle):
+    """A loaded chunk is remeshed once its 26 neighbours are resident (kGenerate queues kMesh for
+    itself; kMesh waits for the neighbours); a marked neighbour that waited is remeshed when the
+    missing chunk arrives; an unloaded chunk's pending remesh is dropped."""
+    from hypercraft_gb300 import batch, world as hw
+    w = hw.edit_world()
+    m = w.index(3, 2, 3)    # missing at first
+    a = w.index(4, 2, 3)    # loaded first: waits for m
+    b = w.index(5, 2, 5)    # loaded, then unloaded before the remesh (no neighbour of m or a)
+    resident = np.ones(w.n_chunks, bool)
+    resident[[m, a, b]] = False
+    rw = hw.ResidentWorld(ctx, w, resident=resident)
+    arena = batch.Arena(4_000_000, 8192, w.n_chunks)
+
+    rw.load([a])
+    cells, _, _ = rw.remesh(arena)
+    assert len(cells) == 0, "a waits for m"
+
+    rw.load([m])
+    cells, _, _ = rw.remesh(arena)
+    assert list(cells) == sorted([m, a])
+    host = arena.host()
+    for i, c in enumerate(cells):
+        want = _meshes_of_chunk(oracle, w, c)
+        got = arena.chunk_meshes(i, host)
+        assert len(got) == len(want) and all(x == y for x, y in zip(got, want)), int(c)
+
+    rw.load([b])
+    rw.unload([b])
+    cells, _, _ = rw.remesh(arena)
+    assert len(cells) == 0, "b's pending remesh was dropped with it"
+
+    rw.load([b])
+    rw.unload([a])
+    rw.load([a])  # the same cell leaves and returns between two remeshes: remeshed once
+    cells, _, _ = rw.remesh(arena)
+    assert list(cells) == sorted([a, b])
+    host = arena.host()
+    for i, c in enumerate(cells):
+        want = _meshes_of_chunk(oracle, w, c)
+        got = arena.chunk_meshes(i, host)
+        assert len(got) == len(want) and all(x == y for x, y in zip(got, want)), int(c)
+
+
+def test_full_arena_requeues_only_what_did_not_fit(ctx, oracle):
+    """Chunks that do not fit the arena stay marked and are remeshed by the next call; the ones
+    that fit are the reference's meshes."""
+    from hypercraft_gb300 import batch, world as hw
+    w = hw.edit_world()
+    resident = np.ones(w.n_chunks, bool)
+    inner = [w.index(x, y, z) for x in (2, 3, 4) for y in (1, 2, 3) for z in (2, 3, 4)]
+    resident[inner] = False
+    rw = hw.ResidentWorld(ctx, w, resident=resident)
+    rw.load(inner)
+    want_quads = sum(len(m.vertices) // 4 for c in inner for m in _meshes_of_chunk(oracle, w, c))
+    small = batch.Arena(want_quads // 2, 8192, w.n_chunks)
+    cells, _, _, status = rw.remesh(small, partial=True)
+    assert sorted(int(c) for c in cells) == sorted(inner)
+    assert 0 < int((status != 0).sum()) < len(cells)
+    host = small.host()
+    for i, c in enumerate(cells):
+        if status[i] == 0:
+            want = _meshes_of_chunk(oracle, w, c)
+            got = small.chunk_meshes(i, host)
+            assert len(got) == len(want) and all(x == y for x, y in zip(got, want)), int(c)
+    big = batch.Arena(4_000_000, 8192, w.n_chunks)
+    again, _, _ = rw.remesh(big)
+    assert sorted(int(c) for c in again) == sorted(int(c) for i, c in enumerate(cells) if status[i] != 0)
+    host = big.host()
+    for i, c in enumerate(again):
+        want = _meshes_of_chunk(oracle, w, c)
+        got = big.chunk_meshes(i, host)
+        assert len(got) == len(want) and all(x == y for x, y in zip(got, want)), int(c)
+    assert len(rw.remesh(big)[0]) == 0
