@@ -39,6 +39,7 @@ def parse():
     ap.add_argument("--workload", default="scale", choices=["scale", "mixture", "edits", "serve"])
     ap.add_argument("--rates", default="2000,5000,10000,20000", help="serve: Poisson arrival rates (requests/s)")
     ap.add_argument("--seconds", type=float, default=3.0, help="serve: trace length per rate")
+    ap.add_argument("--ctas", type=int, default=4, help="serve: CTAs meshing one chunk together (1, 2, 4, 8)")
     ap.add_argument("--size", default="", help="override grid as NXxNYxNZ (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-chunk form (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -387,19 +388,23 @@ def edits_bench(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sp = ctypes_stream(stream)
-    times, cells = [], None
-    for step in range(args.warmup + args.steps):
-        rw.pool.upload(0, w.blocks, w.heights, sp)
-        rw.touch(sp)
-        rw.remesh(arena, sp)  # nothing marked: rebuilds the restored chunks' planes only
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        rw.apply_edits(edits, sp)
-        cells, quads, meshes = rw.remesh(arena, sp)
-        torch.cuda.synchronize()
-        if step >= args.warmup:
-            times.append(time.perf_counter() - t0)
-    ms = 1e3 * float(np.median(times))
+    by_cluster = {}
+    for cluster in (1, 4):
+        rw.set_cluster(cluster)
+        times, cells = [], None
+        for step in range(args.warmup + args.steps):
+            rw.pool.upload(0, w.blocks, w.heights, sp)
+            rw.touch(sp)
+            rw.remesh(arena, sp)  # nothing marked: rebuilds the restored chunks' planes only
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rw.apply_edits(edits, sp)
+            cells, quads, meshes = rw.remesh(arena, sp)
+            torch.cuda.synchronize()
+            if step >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        by_cluster[cluster] = 1e3 * float(np.median(times))
+    ms = min(by_cluster.values())
     # CPU: the reference's kMesh runner over the same remeshed chunks, all host cores
     wc = hw.edit_world()
     from oracle import edits as oe
@@ -413,7 +418,7 @@ def edits_bench(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "workload": "edits: 4096 seeded edits within 48 voxels of the centre of 7x5x7 terrain chunks",
             "remeshed_chunks_per_step": int(len(cells)), "quads_per_step": int(quads),
-            "remesh_latency_ms": ms,
+            "remesh_latency_ms": ms, "latency_ms_by_ctas_per_chunk": by_cluster,
             "cpu_baseline": {"value": len(edits) / dt, "unit": "edits/s", "cores": threads, "kind": kind,
                              "sample": f"kMesh of the same {len(cells)} chunks ({dt * 1e3:.1f} ms), edit application excluded"}}
     print(json.dumps(line), flush=True)
@@ -445,7 +450,7 @@ def serve_bench(args):
         init = wl.initial_loads()
         reqs, times = wl.trace(rate, args.seconds)
         srv = hs.Server(ctx, wl.grid, wl.origin, pool_capacity=0, tick_us=1000, depth=3, max_edits_per_tick=16384,
-                        max_loads_per_tick=512, arena_quads=8 << 20, arena_meshes=1 << 16)
+                        max_loads_per_tick=512, arena_quads=8 << 20, arena_meshes=1 << 16, ctas_per_chunk=args.ctas)
         srv.submit(init)
         srv.drain()
         st0 = srv.stats()
@@ -483,7 +488,7 @@ def serve_bench(args):
             "data": "synthetic: seeded serving trace (the reference publishes no benchmark data)",
             "config": {"workload": "serve: " + (serve_bench.__doc__ or "").split("\n")[0],
                        "rates": [r["rate"] for r in rows], "seconds_per_rate": args.seconds,
-                       "tick_us": 1000, "passes_in_flight": 3},
+                       "tick_us": 1000, "passes_in_flight": 3, "ctas_per_chunk": args.ctas},
             "rates": rows, "clocks": clocks}
     print(json.dumps(line), flush=True)
 

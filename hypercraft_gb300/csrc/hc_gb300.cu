@@ -184,6 +184,39 @@ __global__ void __launch_bounds__(kThreads, 1)
 	}
 }
 
+// Batched form for latency: clusters of `csize` CTAs take chunks from the work counter and mesh
+// each chunk together (mesh_chunk_cta with a Split), so a pass of few heavy chunks finishes sooner.
+__global__ void __launch_bounds__(kThreads, 1)
+    k_mesh_cluster(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes,
+                   uint32_t pool_cap, const int32_t *nbr, uint32_t n, const uint32_t *n_dev, unsigned int *work,
+                   unsigned int *failed, DevTables T, Arena A, const uint8_t *light, const int32_t *nbr_local,
+                   int csize) {
+	namespace cg = cooperative_groups;
+	cg::cluster_group cl = cg::this_cluster();
+	const int rank = (int)cl.block_rank();
+	Smem &S = smem();
+	__shared__ uint32_t s_item;
+	if (n_dev)
+		n = *n_dev;
+	for (;;) {
+		if (rank == 0 && threadIdx.x == 0)
+			s_item = atomicAdd(work, 1u);
+		cl.sync();
+		const uint32_t item = *cl.map_shared_rank(&s_item, 0);
+		cl.sync(); // every CTA has read CTA 0's s_item: CTA 0 may now exit, or claim the next chunk
+		if (item >= n)
+			break;
+		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, light, nbr_local)) {
+			mesh_chunk_cta(S, T, A, item, Split{csize, rank});
+			if (rank == 0 && threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
+				atomicAdd(failed, 1u);
+		} else if (rank == 0) {
+			bad_item(A, item, failed);
+		}
+		cl.sync(); // every CTA has read s_item and finished with the others' shared memory
+	}
+}
+
 // Plain form at scale: one launch per chunk.
 __global__ void __launch_bounds__(kThreads, 1)
     k_mesh_item(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
@@ -224,6 +257,7 @@ struct hc_batch_plan {
 	int32_t *d_nb6 = nullptr;       // per batch chunk: its six face neighbours in the batch, or -1
 	int32_t *d_nbr_local = nullptr; // n x 27: the neighbour table in batch chunk numbers
 	uint32_t *d_levels = nullptr;   // per batch chunk: 2 channels x 15 level planes
+	uint32_t *d_edges = nullptr;    // per batch chunk: their x = 0 and x = 31 bits
 	uint8_t *d_light = nullptr;     // per batch chunk: 32768 light bytes
 	unsigned long long *d_state = nullptr; // quad cursor, mesh cursor, work counter, failed chunks
 	unsigned long long *h_state = nullptr; // pinned
@@ -455,6 +489,8 @@ hc_status hc_ctx_create(int device, hc_ctx **out) {
 		    cudaFuncSetAttribute(k_mesh_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes) !=
 		        cudaSuccess ||
 		    cudaFuncSetAttribute(k_mesh_item, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes) !=
+		        cudaSuccess ||
+		    cudaFuncSetAttribute(k_mesh_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_bytes) !=
 		        cudaSuccess) {
 			s = fail(ctx, HC_ERR_NO_DEVICE, "cannot reserve " + std::to_string(ctx->smem_bytes) + " B of shared memory");
 			break;
@@ -746,6 +782,8 @@ cudaError_t plan_light_tables(hc_batch_plan *p, const std::vector<int32_t> &tabl
 	if (e == cudaSuccess)
 		e = cudaMalloc(&p->d_levels, (size_t)m * kLevelSlotWords * sizeof(uint32_t));
 	if (e == cudaSuccess)
+		e = cudaMalloc(&p->d_edges, (size_t)m * kEdgeSlotWords * sizeof(uint32_t));
+	if (e == cudaSuccess)
 		e = cudaMalloc(&p->d_light, (size_t)m * 32768);
 	return e;
 }
@@ -761,11 +799,11 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		HC_CUDA(ctx, cudaGetLastError());
 	}
 	if (p->d_light) {
-		const LightPass L{p->d_slots, p->d_nb6, p->pool->d_planes, p->pool->d_blocks, p->d_levels, p->d_light, p->n_slots};
-		const uint64_t rows = (uint64_t)p->n_slots * kPlaneWords;
-		const int blocks = (int)std::min<uint64_t>((rows + 255) / 256, (uint64_t)p->grid * 16);
+		const LightPass L{p->d_slots,  p->d_nb6,   p->pool->d_planes, p->pool->d_blocks,
+		                  p->d_levels, p->d_edges, p->d_light,        p->n_slots};
+		const int blocks = (int)std::min<uint64_t>(2ull * p->n_slots, (uint64_t)p->grid * 32);
 		for (int t = kLevels; t >= 1; --t) {
-			k_light_level<<<blocks, 256, 0, st>>>(L, tables(ctx), t);
+			k_light_level<<<blocks, kLightThreads, 0, st>>>(L, tables(ctx), t);
 			HC_CUDA(ctx, cudaGetLastError());
 		}
 	}
@@ -876,6 +914,7 @@ void hc_batch_plan_destroy(hc_batch_plan *plan) {
 	cudaFree(plan->d_nb6);
 	cudaFree(plan->d_nbr_local);
 	cudaFree(plan->d_levels);
+	cudaFree(plan->d_edges);
 	cudaFree(plan->d_light);
 	cudaFree(plan->d_state);
 	cudaFreeHost(plan->h_state);
@@ -954,12 +993,16 @@ struct hc_world {
 	int32_t *d_dirty_list = nullptr, *d_flood_list = nullptr, *d_hchg_list = nullptr, *d_stale_list = nullptr;
 	int32_t *d_list = nullptr, *d_nbr = nullptr;
 	hc_edit *d_edits = nullptr;
+	uint2 *d_sorted = nullptr;                  // one edit batch sorted by voxel, last edit of each voxel
+	uint32_t *d_nsorted = nullptr;
 	int32_t *d_stage = nullptr;                 // staged load/unload positions and slots
 	unsigned long long *d_state = nullptr;      // arena cursors, work counter, failed count
 	uint32_t *h_counts = nullptr;               // pinned
 	unsigned long long *h_state = nullptr;      // pinned
 	int32_t *h_stage = nullptr;                 // pinned, kStageChunks * 4
 	int sms = 0;
+	int cluster = 4;       // CTAs meshing one chunk (1: the one-CTA kernel)
+	int cluster_grid = 0;  // CTAs of the cluster kernel's persistent grid
 };
 
 namespace hc {
@@ -987,7 +1030,10 @@ hc_status world_enqueue_edits(hc_world *w, const hc_edit *d_edits, uint32_t n, c
 	hc_ctx *ctx = w->ctx;
 	const WorldDev W = world_dev(w);
 	for (uint32_t first = 0; first < n; first += kEditBatch) {
-		k_apply_edits<<<1, kEditThreads, 0, st>>>(d_edits + first, std::min<uint32_t>(kEditBatch, n - first), W);
+		k_sort_edits<<<1, kEditThreads, 0, st>>>(d_edits + first, std::min<uint32_t>(kEditBatch, n - first), W,
+		                                         w->d_sorted, w->d_nsorted);
+		HC_CUDA(ctx, cudaGetLastError());
+		k_apply_sorted<<<std::min(w->sms * 2, (int)((n - first + 255) / 256)), 256, 0, st>>>(w->d_sorted, w->d_nsorted, W);
 		HC_CUDA(ctx, cudaGetLastError());
 	}
 	return HC_OK;
@@ -1023,6 +1069,31 @@ hc_status world_enqueue_evict(hc_world *w, const int32_t *d_pos, uint32_t n, cud
 
 Arena world_arena(const hc_world *w, const hc_batch_arena *arena);
 
+cudaLaunchConfig_t cluster_config(dim3 grid, size_t smem, cudaStream_t st, cudaLaunchAttribute *attr, int csize) {
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = grid;
+	cfg.blockDim = dim3(kThreads);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = st;
+	attr[0].id = cudaLaunchAttributeClusterDimension;
+	attr[0].val.clusterDim.x = (unsigned)csize;
+	attr[0].val.clusterDim.y = 1;
+	attr[0].val.clusterDim.z = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	return cfg;
+}
+
+// CTAs of a persistent grid of the cluster kernel: as many clusters as fit at once.
+int cluster_grid_size(hc_ctx *ctx, int csize, int sms) {
+	cudaLaunchAttribute attr[1];
+	cudaLaunchConfig_t cfg = cluster_config(dim3(csize * ((sms + csize - 1) / csize)), ctx->smem_bytes, nullptr, attr, csize);
+	int clusters = 0;
+	if (cudaOccupancyMaxActiveClusters(&clusters, k_mesh_cluster, &cfg) != cudaSuccess || clusters < 1)
+		clusters = std::max(1, sms / csize);
+	return clusters * csize;
+}
+
 hc_status world_enqueue_remesh(hc_world *w, const hc_batch_arena *arena, cudaStream_t st) {
 	hc_ctx *ctx = w->ctx;
 	const WorldDev W = world_dev(w);
@@ -1032,10 +1103,21 @@ hc_status world_enqueue_remesh(hc_world *w, const hc_batch_arena *arena, cudaStr
 	k_collect<<<1, kEditThreads, kCollectSort * sizeof(uint32_t), st>>>(W, w->d_list, w->d_nbr);
 	HC_CUDA(ctx, cudaGetLastError());
 	HC_CUDA(ctx, cudaMemsetAsync(w->d_state, 0, 4 * sizeof(unsigned long long), st));
-	k_mesh_batch<<<w->sms, kThreads, ctx->smem_bytes, st>>>(
-	    w->pool->d_blocks, w->pool->d_heights, w->pool->d_planes, w->pool->capacity, w->d_nbr, 0u,
-	    w->d_counts + kCountRemesh, reinterpret_cast<unsigned int *>(w->d_state + 2),
-	    reinterpret_cast<unsigned int *>(w->d_state + 3), tables(ctx), A, nullptr, nullptr);
+	unsigned int *work = reinterpret_cast<unsigned int *>(w->d_state + 2);
+	unsigned int *failed = reinterpret_cast<unsigned int *>(w->d_state + 3);
+	if (w->cluster > 1) {
+		cudaLaunchAttribute attr[1];
+		cudaLaunchConfig_t cfg = cluster_config(dim3(w->cluster_grid), ctx->smem_bytes, st, attr, w->cluster);
+		HC_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_mesh_cluster, (const uint16_t *)w->pool->d_blocks,
+		                                (const int8_t *)w->pool->d_heights, (const uint32_t *)w->pool->d_planes,
+		                                w->pool->capacity, (const int32_t *)w->d_nbr, 0u,
+		                                (const uint32_t *)(w->d_counts + kCountRemesh), work, failed, tables(ctx), A,
+		                                (const uint8_t *)nullptr, (const int32_t *)nullptr, w->cluster));
+	} else {
+		k_mesh_batch<<<w->sms, kThreads, ctx->smem_bytes, st>>>(
+		    w->pool->d_blocks, w->pool->d_heights, w->pool->d_planes, w->pool->capacity, w->d_nbr, 0u,
+		    w->d_counts + kCountRemesh, work, failed, tables(ctx), A, nullptr, nullptr);
+	}
 	HC_CUDA(ctx, cudaGetLastError());
 	k_requeue<<<list_grid(w), 256, 0, st>>>(W, w->d_list, A.results);
 	HC_CUDA(ctx, cudaGetLastError());
@@ -1115,6 +1197,7 @@ hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc,
 	w->flood_words = (uint32_t)(desc->nx * desc->nz) * 1024u;
 	w->dirty_cap = (uint32_t)cells + kDirtySlack;
 	cudaDeviceGetAttribute(&w->sms, cudaDevAttrMultiProcessorCount, ctx->device);
+	w->cluster_grid = cluster_grid_size(ctx, w->cluster, w->sms);
 	cudaError_t e = cudaFuncSetAttribute(k_collect, cudaFuncAttributeMaxDynamicSharedMemorySize,
 	                                     (int)(kCollectSort * sizeof(uint32_t)));
 	const auto A = [&](void **p, size_t bytes) {
@@ -1135,6 +1218,8 @@ hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc,
 	A((void **)&w->d_list, cells * sizeof(int32_t));
 	A((void **)&w->d_nbr, cells * 27 * sizeof(int32_t));
 	A((void **)&w->d_edits, kEditBatch * sizeof(hc_edit));
+	A((void **)&w->d_sorted, kEditBatch * sizeof(uint2));
+	A((void **)&w->d_nsorted, sizeof(uint32_t));
 	A((void **)&w->d_stage, kStageChunks * 4 * sizeof(int32_t));
 	A((void **)&w->d_state, 4 * sizeof(unsigned long long));
 	if (e == cudaSuccess)
@@ -1166,7 +1251,8 @@ void hc_world_destroy(hc_world *w) {
 	cudaSetDevice(w->ctx->device);
 	for (void *p : {(void *)w->d_slots, (void *)w->d_flags, (void *)w->d_flood, (void *)w->d_stale, (void *)w->d_counts,
 	                (void *)w->d_dirty_list, (void *)w->d_flood_list, (void *)w->d_hchg_list, (void *)w->d_stale_list,
-	                (void *)w->d_list, (void *)w->d_nbr, (void *)w->d_edits, (void *)w->d_stage, (void *)w->d_state})
+	                (void *)w->d_list, (void *)w->d_nbr, (void *)w->d_edits, (void *)w->d_sorted, (void *)w->d_nsorted,
+	                (void *)w->d_stage, (void *)w->d_state})
 		cudaFree(p);
 	cudaFreeHost(w->h_counts);
 	cudaFreeHost(w->h_state);
@@ -1240,6 +1326,14 @@ hc_status hc_world_unload(hc_world *w, const int32_t *positions, uint32_t n, voi
 			return s;
 		HC_CUDA(ctx, cudaStreamSynchronize(st));
 	}
+	return HC_OK;
+}
+
+hc_status hc_world_set_cluster(hc_world *w, int ctas_per_chunk) {
+	if (!w || (ctas_per_chunk != 1 && ctas_per_chunk != 2 && ctas_per_chunk != 4 && ctas_per_chunk != 8))
+		return HC_ERR_INVALID_ARG;
+	w->cluster = ctas_per_chunk;
+	w->cluster_grid = ctas_per_chunk > 1 ? cluster_grid_size(w->ctx, ctas_per_chunk, w->sms) : 0;
 	return HC_OK;
 }
 

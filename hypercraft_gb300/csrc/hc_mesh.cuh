@@ -18,9 +18,21 @@
 // output order, which gives every quad its final stream index k before anything is written, so
 // all quads are written in parallel straight to their reference positions.
 #pragma once
+#include <cooperative_groups.h>
+
 #include "hc_relight.cuh"
 
 namespace hc {
+
+// How the face planes of one chunk are shared by the CTAs of a thread-block cluster (a chunk
+// meshed by several SMs, for latency): CTA `rank` of `c` owns the slices axis * 33 + slice that
+// are congruent to rank mod c, with both face directions of each. Every CTA stages the whole chunk.
+struct Split {
+	int c, rank;
+	__device__ __forceinline__ int planes() const { return 2 * ((kSlices - rank + c - 1) / c); }
+	__device__ __forceinline__ int plane(int j) const { return 2 * (rank + c * (j >> 1)) + (j & 1); }
+	__device__ __forceinline__ int owner(int p) const { return (p >> 1) % c; }
+};
 
 struct Emit {
 	uint2 *verts;
@@ -283,9 +295,10 @@ __device__ void plane_visibility(Smem &S) {
 
 // Pass 1b: exact Show for the complex candidates of every plane row (texture lookups, dynamic
 // liquid textures), and transparent-pass bits of the faces it shows. Lane = plane row.
-__device__ void plane_complex(Smem &S) {
+__device__ void plane_complex(Smem &S, const Split &sp) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int p = warp; p < kPlanes; p += kWarps) {
+	for (int j = warp; j < sp.planes(); j += kWarps) {
+		const int p = sp.plane(j);
 		uint32_t *m = S.u.masks[p][lane];
 		uint32_t cx = m[1];
 		if (!__any_sync(0xffffffffu, cx != 0))
@@ -362,9 +375,10 @@ __device__ __forceinline__ Key face_key(const Smem &S, int a, int s, int inv, in
 // faces of a plane are taken in batches of whole rows (at most 32 faces), one face per lane, so
 // the light keys are computed by full warps; a face's right neighbour is the next lane and its
 // upper neighbour sits in this batch or in the previous one.
-__device__ void plane_keys(Smem &S) {
+__device__ void plane_keys(Smem &S, const Split &sp) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int p = warp; p < kPlanes; p += kWarps) {
+	for (int j = warp; j < sp.planes(); j += kWarps) {
+		const int p = sp.plane(j);
 		uint32_t *mrow = S.u.masks[p][lane];
 		const uint32_t N = mrow[0];
 		mrow[1] = 0;
@@ -485,10 +499,11 @@ __device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, 
 
 // Counts the quads of every plane (warp per plane) and keeps their records in shared memory while
 // they fit; misc[4] = records kept, misc[5] = 1 if some did not fit.
-__device__ void planes_count(Smem &S) {
+__device__ void planes_count(Smem &S, const Split &sp) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t lt = (1u << lane) - 1u;
-	for (int p = warp; p < kPlanes; p += kWarps) {
+	for (int j = warp; j < sp.planes(); j += kWarps) {
+		const int p = sp.plane(j);
 		uint32_t n_all = 0, n_st[2] = {0, 0};
 		warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
 			const uint32_t cnt = __popc(starts);
@@ -554,7 +569,7 @@ __device__ __forceinline__ void emit_record(Smem &S, const Emit &E, uint2 r) {
 // Emits the plane quads. Normally planes_count kept all their records; otherwise the quads are
 // taken in windows of kQuadBuf (in output order), the planes overlapping a window re-run their
 // merge to stage that window's records, and the CTA writes them.
-__device__ void planes_emit(Smem &S, const Emit &E, uint32_t custom_all, uint32_t plane_quads) {
+__device__ void planes_emit(Smem &S, const Emit &E, uint32_t custom_all, uint32_t plane_quads, const Split &sp) {
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	if (!S.misc[5]) {
 		for (uint32_t j = tid; j < S.misc[4]; j += kThreads)
@@ -563,7 +578,13 @@ __device__ void planes_emit(Smem &S, const Emit &E, uint32_t custom_all, uint32_
 	}
 	const uint32_t lt = (1u << lane) - 1u;
 	for (uint32_t w0 = 0; w0 < plane_quads; w0 += kQuadBuf) {
-		for (int p = warp; p < kPlanes; p += kWarps) {
+		if (sp.c > 1) { // other CTAs' quads of this window stay unfilled here
+			for (int j = tid; j < kQuadBuf; j += kThreads)
+				S.aux.quads[j].x = 0xffffffffu;
+			__syncthreads();
+		}
+		for (int j = warp; j < sp.planes(); j += kWarps) {
+			const int p = sp.plane(j);
 			const uint32_t pb = S.seg_base[2][1 + p] - custom_all;
 			const uint32_t pc = S.seg_cnt[0][1 + p] + S.seg_cnt[1][1 + p];
 			if (!pc || pb >= w0 + kQuadBuf || pb + pc <= w0)
@@ -586,7 +607,8 @@ __device__ void planes_emit(Smem &S, const Emit &E, uint32_t custom_all, uint32_
 		__syncthreads();
 		const uint32_t n = min((uint32_t)kQuadBuf, plane_quads - w0);
 		for (uint32_t j = tid; j < n; j += kThreads)
-			emit_record(S, E, S.aux.quads[j]);
+			if (S.aux.quads[j].x != 0xffffffffu)
+				emit_record(S, E, S.aux.quads[j]);
 		__syncthreads();
 	}
 }
@@ -679,21 +701,31 @@ struct Arena {
 
 enum : uint32_t { kChunkOk = 0, kChunkCapacity = 1 };
 
-// Relights and meshes one chunk whose 27 neighbour pointers are already in S.blk / S.hgt / S.pln.
-__device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint32_t pos) {
+// Relights and meshes one chunk whose 27 neighbour pointers are already in S.blk / S.hgt / S.pln
+// (and S.lgt). With sp.c > 1 the c CTAs of a cluster mesh it together: each stages it, owns a
+// share of the face planes, and they exchange per-plane counts, the arena reservation and the
+// meshes' bounding boxes through distributed shared memory; CTA 0 writes the results and the
+// mesh descriptors. Every CTA of the cluster must call this with the same chunk.
+__device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint32_t pos, Split sp = Split{1, 0}) {
+	namespace cg = cooperative_groups;
 	const int tid = threadIdx.x;
+	const bool lead = sp.rank == 0;
 	for (int i = tid; i < 2 * kMaxMeshesPerStream; i += kThreads) {
 		uint32_t *bb = S.aabb[i / kMaxMeshesPerStream][i % kMaxMeshesPerStream];
 		bb[0] = bb[1] = bb[2] = 0xffffffffu;
 		bb[3] = bb[4] = bb[5] = 0u;
+		S.trig[i / kMaxMeshesPerStream][i % kMaxMeshesPerStream] = 0xffffffffu;
 	}
+	for (int i = tid; i < 2 * (kSegments + 1); i += kThreads)
+		S.seg_cnt[i / (kSegments + 1)][i % (kSegments + 1)] = 0;
 	const bool blank = stage_classes(S, T);
 
 	uint32_t qo = 0, qt = 0;
 	uint32_t eo = 0, et = 0;
 	if (!blank) {
-		uint32_t co, ct, to, tt;
-		custom_count(S, tid * kBlocksPerThread, co, ct);
+		uint32_t co = 0, ct = 0, to, tt;
+		if (lead)
+			custom_count(S, tid * kBlocksPerThread, co, ct);
 		block_scan2(S, co, ct, eo, et, to, tt);
 		if (S.lgt[26])
 			light_from_batch(S);
@@ -702,9 +734,9 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		__syncthreads();
 		plane_visibility(S);
 		__syncthreads();
-		plane_complex(S);
+		plane_complex(S, sp);
 		__syncthreads();
-		plane_keys(S);
+		plane_keys(S, sp);
 		if (tid == 0) {
 			S.seg_cnt[0][0] = to;
 			S.seg_cnt[1][0] = tt;
@@ -712,8 +744,21 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 			S.misc[5] = 0;
 		}
 		__syncthreads();
-		planes_count(S);
+		planes_count(S, sp);
 		__syncthreads();
+		if (sp.c > 1) { // every CTA takes the counts of the segments the others own
+			cg::cluster_group cl = cg::this_cluster();
+			cl.sync();
+			for (int i = tid; i < kSegments; i += kThreads) {
+				const int owner = i == 0 ? 0 : sp.owner(i - 1);
+				if (owner != sp.rank) {
+					const uint32_t *src = cl.map_shared_rank(&S.seg_cnt[0][0], owner);
+					S.seg_cnt[0][i] = src[i];
+					S.seg_cnt[1][i] = src[(kSegments + 1) + i];
+				}
+			}
+			__syncthreads();
+		}
 		segment_scan(S);
 		__syncthreads();
 		qo = S.misc[0];
@@ -722,31 +767,52 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 
 	const uint32_t q = qo + qt;
 	const uint32_t mo = (qo + kQuadsPerMesh - 1) / kQuadsPerMesh, mt = (qt + kQuadsPerMesh - 1) / kQuadsPerMesh;
-	__shared__ unsigned long long s_q0;
-	__shared__ unsigned int s_m0;
-	__shared__ uint32_t s_status;
-	if (tid == 0) {
-		s_q0 = q ? atomicAdd(A.quad_cursor, (unsigned long long)q) : 0ull;
-		s_m0 = (mo + mt) ? atomicAdd(A.mesh_cursor, mo + mt) : 0u;
-		s_status = (s_q0 + q > A.quad_cap || s_m0 + mo + mt > A.mesh_cap) ? kChunkCapacity : kChunkOk;
+	if (lead && tid == 0) {
+		const unsigned long long q0 = q ? atomicAdd(A.quad_cursor, (unsigned long long)q) : 0ull;
+		const unsigned int m0 = (mo + mt) ? atomicAdd(A.mesh_cursor, mo + mt) : 0u;
+		const uint32_t status = (q0 + q > A.quad_cap || m0 + mo + mt > A.mesh_cap) ? kChunkCapacity : kChunkOk;
+		S.misc[8] = (uint32_t)q0, S.misc[9] = (uint32_t)(q0 >> 32), S.misc[10] = m0, S.misc[11] = status;
+		uint32_t *r = A.results + 5 * pos;
+		r[0] = qo, r[1] = qt, r[2] = m0, r[3] = mo + mt, r[4] = status;
+	}
+	if (sp.c > 1 && !blank) { // the reservation of CTA 0
+		cg::cluster_group cl = cg::this_cluster();
+		cl.sync();
+		if (!lead && tid < 4)
+			S.misc[8 + tid] = cl.map_shared_rank(&S.misc[0], 0)[8 + tid];
 	}
 	__syncthreads();
-	const unsigned long long q0 = s_q0;
-	const unsigned int m0 = s_m0;
-	if (tid == 0) {
-		uint32_t *r = A.results + 5 * pos;
-		r[0] = qo, r[1] = qt, r[2] = m0, r[3] = mo + mt, r[4] = s_status;
-	}
-	if (q == 0 || s_status != kChunkOk)
+	const unsigned long long q0 = (unsigned long long)S.misc[8] | ((unsigned long long)S.misc[9] << 32);
+	const unsigned int m0 = S.misc[10];
+	if (blank || q == 0 || S.misc[11] != kChunkOk)
 		return;
 
 	const Emit E{A.verts, A.idx, q0, qo};
-	custom_emit(S, E, tid * kBlocksPerThread, eo, et, eo + et);
+	if (lead)
+		custom_emit(S, E, tid * kBlocksPerThread, eo, et, eo + et);
 	const uint32_t custom_all = S.seg_base[2][1];
-	planes_emit(S, E, custom_all, q - custom_all);
+	planes_emit(S, E, custom_all, q - custom_all, sp);
+
+	if (sp.c > 1) { // CTA 0 merges the boxes and closing positions of every CTA's quads
+		cg::cluster_group cl = cg::this_cluster();
+		__syncthreads();
+		cl.sync();
+		if (lead)
+			for (int i = tid; i < 2 * kMaxMeshesPerStream; i += kThreads) {
+				const int st = i / kMaxMeshesPerStream, m = i % kMaxMeshesPerStream;
+				uint32_t *bb = S.aabb[st][m];
+				for (int r = 1; r < sp.c; ++r) {
+					const uint32_t *o = cl.map_shared_rank(&S.aabb[st][m][0], r);
+					bb[0] = min(bb[0], o[0]), bb[1] = min(bb[1], o[1]), bb[2] = min(bb[2], o[2]);
+					bb[3] = max(bb[3], o[3]), bb[4] = max(bb[4], o[4]), bb[5] = max(bb[5], o[5]);
+					S.trig[st][m] = min(S.trig[st][m], cl.map_shared_rank(&S.trig[st][m], r)[0]);
+				}
+			}
+		__syncthreads();
+	}
 
 	// Mesh descriptors: closed meshes in closing order, then the open opaque and transparent ones.
-	if (tid == 0) {
+	if (lead && tid == 0) {
 		uint32_t io = 0, it = 0, out = m0;
 		const auto put = [&](int st, uint32_t j, uint32_t nst) {
 			const uint32_t first = j * kQuadsPerMesh, n = min((uint32_t)kQuadsPerMesh, nst - first);

@@ -308,6 +308,8 @@ __device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hg
 
 constexpr int kLevels = 15;
 constexpr size_t kLevelSlotWords = (size_t)2 * kLevels * kPlaneWords; // per chunk: 2 channels x 15 levels
+constexpr size_t kEdgeSlotWords = (size_t)2 * kLevels * 2 * 32;       // per chunk: x = 0 and x = 31 bits
+constexpr int kLightThreads = 512;                                     // two blocks per chunk
 
 struct LightPass {
 	const int32_t *slots;   // batch chunk -> pool slot
@@ -315,12 +317,16 @@ struct LightPass {
 	const uint32_t *planes; // pool planes (pass, sun, level-15 emitters, low-emitter rows)
 	const uint16_t *blocks; // pool blocks (rows with emitters below 15)
 	uint32_t *levels;       // batch chunk -> channel -> level t at plane t - 1 -> 1024 rows
+	uint32_t *edges;        // batch chunk -> channel -> level -> {bit x = 0, bit x = 31} of every row
 	uint8_t *light;         // batch chunk -> 32768 cells (sun | torch << 4), the reference's cell order
 	uint32_t n;             // batch chunks
 };
 
 __device__ __forceinline__ const uint32_t *level_plane(const LightPass &L, int i, int c, int t) {
 	return L.levels + (size_t)i * kLevelSlotWords + (size_t)(c * kLevels + t - 1) * kPlaneWords;
+}
+__device__ __forceinline__ const uint32_t *level_edges(const LightPass &L, int i, int c, int t) {
+	return L.edges + (size_t)i * kEdgeSlotWords + (size_t)(c * kLevels + t - 1) * 64;
 }
 
 __device__ __forceinline__ uint32_t mux(uint32_t c, uint32_t a, uint32_t b) { return (c & a) | (~c & b); }
@@ -334,53 +340,68 @@ __device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
 	           mux(b[2], mux(b[1], s[6], s[4]), mux(b[1], s[2], s[0])));
 }
 
-// Level t of every row of every batch chunk (one thread per row, both channels); level 1 also
-// writes the cells' light bytes.
-__global__ void __launch_bounds__(256) k_light_level(LightPass L, DevTables T, int t) {
-	const uint64_t total = (uint64_t)L.n * kPlaneWords;
-	for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x) {
-		const int i = (int)(g >> 10), r = (int)(g & 1023u), y = r >> 5, z = r & 31;
-		const uint32_t *P = L.planes + (size_t)L.slots[i] * kPlaneStride;
+// Level t of every batch chunk: a block of kLightThreads rows (half a chunk), one row per thread,
+// both channels, every load independent; also the row edge bits the x neighbours read at the next
+// level. Level 1 also writes the cells' light bytes.
+__global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevTables T, int t) {
+	__shared__ int s_nb[6];
+	__shared__ int32_t s_slot;
+	const int tid = threadIdx.x, lane = tid & 31;
+	for (uint32_t blk = blockIdx.x; blk < 2 * L.n; blk += gridDim.x) {
+		const int i = (int)(blk >> 1), r = (int)(blk & 1u) * kLightThreads + tid, y = r >> 5, z = r & 31;
+		if (tid < 6)
+			s_nb[tid] = __ldg(L.nb6 + 6 * i + tid);
+		if (tid == 6)
+			s_slot = __ldg(L.slots + i);
+		__syncthreads();
+		const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
 		uint32_t s[2];
 		if (t == kLevels) {
 			s[0] = __ldg(P + kPlaneSun * kPlaneWords + r);
 			s[1] = __ldg(P + kPlaneT15 * kPlaneWords + r);
 		} else {
-			const int *nb = L.nb6 + 6 * i;
-			const int xm = nb[0], xp = nb[1];
-			const int yi = y > 0 ? i : nb[2], yr = y > 0 ? r - 32 : r + 31 * 32;
-			const int yj = y < 31 ? i : nb[3], yq = y < 31 ? r + 32 : r - 31 * 32;
-			const int zi = z > 0 ? i : nb[4], zr = z > 0 ? r - 1 : r + 31;
-			const int zj = z < 31 ? i : nb[5], zq = z < 31 ? r + 1 : r - 31;
+			const int xm = s_nb[0], xp = s_nb[1];
+			const int yi = y > 0 ? i : s_nb[2], yr = y > 0 ? r - 32 : r + 31 * 32;
+			const int yj = y < 31 ? i : s_nb[3], yq = y < 31 ? r + 32 : r - 31 * 32;
+			const int zi = z > 0 ? i : s_nb[4], zr = z > 0 ? r - 1 : r + 31;
+			const int zj = z < 31 ? i : s_nb[5], zq = z < 31 ? r + 1 : r - 31;
 			const uint32_t pass = __ldg(P + kPlanePass * kPlaneWords + r);
+			uint32_t v[2][7];
 #pragma unroll
 			for (int c = 0; c < 2; ++c) {
-				const uint32_t prev = level_plane(L, i, c, t + 1)[r];
-				uint32_t d = (prev << 1) | (prev >> 1);
-				if (xm >= 0)
-					d |= level_plane(L, xm, c, t + 1)[r] >> 31;
-				if (xp >= 0)
-					d |= level_plane(L, xp, c, t + 1)[r] << 31;
-				if (yi >= 0)
-					d |= level_plane(L, yi, c, t + 1)[yr];
-				if (yj >= 0)
-					d |= level_plane(L, yj, c, t + 1)[yq];
-				if (zi >= 0)
-					d |= level_plane(L, zi, c, t + 1)[zr];
-				if (zj >= 0)
-					d |= level_plane(L, zj, c, t + 1)[zq];
+				v[c][0] = __ldg(level_plane(L, i, c, t + 1) + r);
+				v[c][1] = xm >= 0 ? __ldg(level_edges(L, xm, c, t + 1) + 32 + (r >> 5)) : 0u;
+				v[c][2] = xp >= 0 ? __ldg(level_edges(L, xp, c, t + 1) + (r >> 5)) : 0u;
+				v[c][3] = yi >= 0 ? __ldg(level_plane(L, yi, c, t + 1) + yr) : 0u;
+				v[c][4] = yj >= 0 ? __ldg(level_plane(L, yj, c, t + 1) + yq) : 0u;
+				v[c][5] = zi >= 0 ? __ldg(level_plane(L, zi, c, t + 1) + zr) : 0u;
+				v[c][6] = zj >= 0 ? __ldg(level_plane(L, zj, c, t + 1) + zq) : 0u;
+			}
+#pragma unroll
+			for (int c = 0; c < 2; ++c) {
+				const uint32_t prev = v[c][0];
+				const uint32_t d = (prev << 1) | (prev >> 1) | ((v[c][1] >> (r & 31)) & 1u) |
+				                   (((v[c][2] >> (r & 31)) & 1u) << 31) | v[c][3] | v[c][4] | v[c][5] | v[c][6];
 				s[c] = prev | (pass & d);
 			}
 		}
 		if ((__ldg(P + 3 * kPlaneWords + (r >> 5)) >> (r & 31)) & 1u) { // emitters below level 15 in this row
-			const uint16_t *row = L.blocks + (size_t)L.slots[i] * 32768 + r * 32;
+			const uint16_t *row = L.blocks + (size_t)s_slot * 32768 + r * 32;
 			for (int x = 0; x < 32; ++x)
 				if (T.classes[T.class_of[row[x]]].light >= t)
 					s[1] |= 1u << x;
 		}
-		uint32_t *out0 = L.levels + (size_t)i * kLevelSlotWords + (size_t)(t - 1) * kPlaneWords + r;
-		out0[0] = s[0];
-		out0[(size_t)kLevels * kPlaneWords] = s[1];
+#pragma unroll
+		for (int c = 0; c < 2; ++c) {
+			uint32_t *out = L.levels + (size_t)i * kLevelSlotWords + (size_t)(c * kLevels + t - 1) * kPlaneWords;
+			out[r] = s[c];
+			const uint32_t lo = __ballot_sync(0xffffffffu, s[c] & 1u), hi = __ballot_sync(0xffffffffu, s[c] >> 31);
+			if (lane == 0) {
+				uint32_t *e = L.edges + (size_t)i * kEdgeSlotWords + (size_t)(c * kLevels + t - 1) * 64;
+				e[r >> 5] = lo;
+				e[32 + (r >> 5)] = hi;
+			}
+		}
 		if (t == 1) {
 			uint32_t lv[kLevels], b[2][4];
 #pragma unroll
@@ -388,13 +409,13 @@ __global__ void __launch_bounds__(256) k_light_level(LightPass L, DevTables T, i
 				lv[0] = s[c];
 #pragma unroll
 				for (int u = 2; u <= kLevels; ++u)
-					lv[u - 1] = level_plane(L, i, c, u)[r];
+					lv[u - 1] = __ldg(level_plane(L, i, c, u) + r);
 				level_bits(lv, b[c]);
 			}
 			uint32_t w[8];
 #pragma unroll
 			for (int q = 0; q < 8; ++q) {
-				uint32_t v = 0;
+				uint32_t val = 0;
 #pragma unroll
 				for (int k = 0; k < 4; ++k) {
 					const int x = 4 * q + k;
@@ -402,14 +423,15 @@ __global__ void __launch_bounds__(256) k_light_level(LightPass L, DevTables T, i
 #pragma unroll
 					for (int bit = 0; bit < 4; ++bit)
 						byte |= ((b[0][bit] >> x) & 1u) << bit | ((b[1][bit] >> x) & 1u) << (bit + 4);
-					v |= byte << (8 * k);
+					val |= byte << (8 * k);
 				}
-				w[q] = v;
+				w[q] = val;
 			}
 			uint4 *dst = reinterpret_cast<uint4 *>(L.light + (size_t)i * 32768 + r * 32);
 			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
 			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
 		}
+		__syncthreads(); // s_nb, s_slot are rewritten for the next block
 	}
 }
 

@@ -264,6 +264,8 @@ hc_status start_tick(hc_server *s, uint32_t *taken, bool *ran) {
 	std::lock_guard<std::mutex> step(s->step_mu);
 	*taken = 0, *ran = false;
 	std::unique_lock<std::mutex> lk(s->mu);
+	if (!s->err.empty())
+		return ctx_fail(s->ctx, HC_ERR_CUDA, s->err);
 	if (s->queue.empty() && !s->carry)
 		return HC_OK;
 	s->cv.wait(lk, [&] { return s->next_tick - s->next_done < s->ring.size(); });
@@ -301,8 +303,16 @@ bool finish_tick(hc_server *s, bool block) {
 		tp = &s->ring[s->next_done % s->ring.size()];
 	}
 	TickSlot &t = *tp;
-	cudaEventSynchronize(t.done);
+	const cudaError_t ev = cudaEventSynchronize(t.done);
 	const uint64_t done = now_ns();
+	if (ev != cudaSuccess) { // the pass failed: stop, and report it from every later call
+		std::lock_guard<std::mutex> lk(s->mu);
+		s->err = std::string("device pass failed: ") + cudaGetErrorString(ev);
+		s->running.store(false);
+		++s->next_done;
+		s->cv.notify_all();
+		return true;
+	}
 	float ms = 0.f;
 	cudaEventElapsedTime(&ms, t.start, t.done);
 	const uint32_t n = t.h_counts[kWorldCountRemesh];
@@ -470,7 +480,8 @@ hc_status hc_server_create(hc_ctx *ctx, const hc_world_desc *desc, uint32_t pool
 		return st;
 	}
 	s->cell_slot.assign(cells, -1);
-	if ((st = hc_world_create(ctx, s->pool, desc, s->cell_slot.data(), &s->world)) != HC_OK) {
+	if ((st = hc_world_create(ctx, s->pool, desc, s->cell_slot.data(), &s->world)) != HC_OK ||
+	    (st = hc_world_set_cluster(s->world, config->ctas_per_chunk ? (int)config->ctas_per_chunk : 4)) != HC_OK) {
 		hc_server_destroy(s);
 		return st;
 	}
@@ -580,6 +591,8 @@ hc_status hc_server_step(hc_server *s, uint32_t *admitted) {
 	}
 	if (admitted)
 		*admitted = taken;
+	if (!s->err.empty())
+		return ctx_fail(s->ctx, HC_ERR_CUDA, s->err);
 	return HC_OK;
 }
 

@@ -134,11 +134,31 @@ __device__ __forceinline__ int pow2_at_least(uint32_t n, int lo) {
 	return p;
 }
 
-// Applies up to kEditBatch edits: sorts them by (voxel, order) in shared memory so the last edit of
-// a voxel wins, then writes each distinct voxel once, marking remeshes and floods as
-// ChunkSetBlockTask.cpp:83-107 does for a block that changed.
-__global__ void __launch_bounds__(kEditThreads) k_apply_edits(const hc_edit *edits, uint32_t n, WorldDev W) {
+// Block-wide ordered compaction step: returns this thread's output position among the takers of
+// this pass and advances *base by their number.
+__device__ __forceinline__ uint32_t block_compact(bool take, uint32_t *s_warp, uint32_t &base) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t bal = __ballot_sync(0xffffffffu, take);
+	if (lane == 0)
+		s_warp[warp] = __popc(bal);
+	__syncthreads();
+	uint32_t before = 0, total = 0;
+	for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+		before += w < warp ? s_warp[w] : 0;
+		total += s_warp[w];
+	}
+	const uint32_t pos = base + before + __popc(bal & ((1u << lane) - 1u));
+	__syncthreads();
+	base += total;
+	return pos;
+}
+
+// Sorts up to kEditBatch edits by (voxel, order) in shared memory and keeps the last edit of each
+// voxel: out[0, *n_out) = (cell, voxel | block << 15). One CTA.
+__global__ void __launch_bounds__(kEditThreads) k_sort_edits(const hc_edit *edits, uint32_t n, WorldDev W, uint2 *out,
+                                                             uint32_t *n_out) {
 	__shared__ unsigned long long key[kEditBatch];
+	__shared__ uint32_t s_warp[kEditThreads / 32];
 	const int tid = threadIdx.x;
 	const int p = pow2_at_least(n, 32);
 	for (int i = tid; i < p; i += kEditThreads) {
@@ -158,14 +178,28 @@ __global__ void __launch_bounds__(kEditThreads) k_apply_edits(const hc_edit *edi
 	}
 	__syncthreads();
 	block_bitonic_sort(key, p);
-	for (int i = tid; i < p; i += kEditThreads) {
-		const unsigned long long k = key[i];
-		if (k == ~0ull)
-			continue;
-		if (i + 1 < p && (key[i + 1] >> 12) == (k >> 12))
-			continue; // a later edit of the same voxel wins
-		const int cell = (int)(k >> 27), lidx = (int)((k >> 12) & 32767u), order = (int)(k & 4095u);
-		const uint16_t nb = (uint16_t)(edits[order].block & 0xffffu);
+	uint32_t base = 0;
+	for (int i0 = 0; i0 < p; i0 += kEditThreads) {
+		const int i = i0 + tid;
+		const unsigned long long k = i < p ? key[i] : ~0ull;
+		// a later edit of the same voxel wins
+		const bool take = k != ~0ull && !(i + 1 < p && (key[i + 1] >> 12) == (k >> 12));
+		const uint32_t pos = block_compact(take, s_warp, base);
+		if (take)
+			out[pos] = make_uint2((uint32_t)(k >> 27), (uint32_t)((k >> 12) & 32767u) | ((edits[k & 4095u].block & 0xffffu) << 15));
+	}
+	if (tid == 0)
+		*n_out = base;
+}
+
+// Writes each sorted edit's voxel, marking remeshes and floods as ChunkSetBlockTask.cpp:83-107
+// does for a block that changed. Grid-stride over the sorted edits.
+__global__ void k_apply_sorted(const uint2 *sorted, const uint32_t *n_sorted, WorldDev W) {
+	const uint32_t n = *n_sorted;
+	for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+		const uint2 v = sorted[e];
+		const int cell = (int)v.x, lidx = (int)(v.y & 32767u);
+		const uint16_t nb = (uint16_t)(v.y >> 15);
 		const int32_t slot = W.slots[cell];
 		uint16_t *dst = W.blocks + (size_t)slot * 32768 + lidx;
 		if (*dst == nb)
@@ -296,10 +330,15 @@ __device__ __forceinline__ bool collect_cell(const WorldDev &W, int cell) {
 	}
 	int ix, iy, iz;
 	cell_xyz(W, cell, ix, iy, iz);
-	bool all = true;
-	for (int d = 0; d < 27 && all; ++d) {
-		const int dx = d % 3 - 1, dy = (d / 3) % 3 - 1, dz = d / 9 - 1;
-		all = in_grid(W, ix + dx, iy + dy, iz + dz) && W.slots[cell_of(W, ix + dx, iy + dy, iz + dz)] >= 0;
+	bool all = ix > 0 && iy > 0 && iz > 0 && ix < W.nx - 1 && iy < W.ny - 1 && iz < W.nz - 1;
+	if (all) {
+		int32_t s[27]; // all loads in flight at once
+#pragma unroll
+		for (int d = 0; d < 27; ++d)
+			s[d] = W.slots[cell_of(W, ix + d % 3 - 1, iy + (d / 3) % 3 - 1, iz + d / 9 - 1)];
+#pragma unroll
+		for (int d = 0; d < 27; ++d)
+			all &= s[d] >= 0;
 	}
 	if (all)
 		atomicAnd(W.flags + cell, ~(kCellListed | kCellWaiting));
@@ -315,29 +354,11 @@ __device__ __forceinline__ void write_remesh(const WorldDev &W, int cell, uint32
 	int ix, iy, iz;
 	cell_xyz(W, cell, ix, iy, iz);
 	const int kRev[3] = {1, -1, 0};
+#pragma unroll
 	for (int i = 0; i < 27; ++i) {
 		const int dz = kRev[i % 3], dy = kRev[(i / 3) % 3], dx = kRev[i / 9];
 		nbr[(size_t)pos * 27 + i] = W.slots[cell_of(W, ix + dx, iy + dy, iz + dz)];
 	}
-}
-
-// Block-wide ordered compaction step: returns this thread's output position among the takers of
-// this pass and advances *base by their number.
-__device__ __forceinline__ uint32_t block_compact(bool take, uint32_t *s_warp, uint32_t &base) {
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	const uint32_t bal = __ballot_sync(0xffffffffu, take);
-	if (lane == 0)
-		s_warp[warp] = __popc(bal);
-	__syncthreads();
-	uint32_t before = 0, total = 0;
-	for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-		before += w < warp ? s_warp[w] : 0;
-		total += s_warp[w];
-	}
-	const uint32_t pos = base + before + __popc(bal & ((1u << lane) - 1u));
-	__syncthreads();
-	base += total;
-	return pos;
 }
 
 // Builds the remesh list, in grid order, from the dirty list (sorted in shared memory) or, when

@@ -38,7 +38,7 @@ class _Desc(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("tick_us", ctypes.c_uint32), ("depth", ctypes.c_uint32), ("max_edits_per_tick", ctypes.c_uint32),
                 ("max_loads_per_tick", ctypes.c_uint32), ("arena_quads", ctypes.c_uint64),
-                ("arena_meshes", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("arena_meshes", ctypes.c_uint32), ("ctas_per_chunk", ctypes.c_uint32)]
 
 
 class ServerStats(ctypes.Structure):
@@ -82,11 +82,12 @@ class Server:
 
     def __init__(self, ctx: Context, grid, origin, *, pool_capacity: int = 0, tick_us: int = 1000, depth: int = 3,
                  max_edits_per_tick: int = 16384, max_loads_per_tick: int = 256, arena_quads: int = 4 << 20,
-                 arena_meshes: int = 1 << 15):
+                 arena_meshes: int = 1 << 15, ctas_per_chunk: int = 0):
         self.ctx = ctx
         self.lib = _bind(batch._bind(library()))
         self.grid, self.origin = tuple(grid), tuple(origin)
-        self.cfg = ServerConfig(tick_us, depth, max_edits_per_tick, max_loads_per_tick, arena_quads, arena_meshes, 0)
+        self.cfg = ServerConfig(tick_us, depth, max_edits_per_tick, max_loads_per_tick, arena_quads, arena_meshes,
+                                ctas_per_chunk)
         h = ctypes.c_void_p()
         ctx.check(self.lib.hc_server_create(ctx.handle, ctypes.byref(_Desc(*self.grid, *self.origin)), pool_capacity,
                                             ctypes.byref(self.cfg), ctypes.byref(h)), "hc_server_create")

@@ -38,6 +38,7 @@ def _bind(lib):
     lib.hc_world_load.argtypes = [vp, P(ChunkLoad), ctypes.c_uint32, vp]
     lib.hc_world_unload.argtypes = [vp, vp, ctypes.c_uint32, vp]
     lib.hc_world_touch.argtypes = [vp, vp]
+    lib.hc_world_set_cluster.argtypes = [vp, ctypes.c_int]
     lib._world_bound = True
     return lib
 
@@ -88,6 +89,10 @@ class ResidentWorld:
         pos = np.array([[o + c for o, c in zip(self.world.origin, self.world.coords(int(i)))] for i in cells],
                        np.int32).reshape(-1, 3)
         self.ctx.check(self.lib.hc_world_unload(self.handle, pos.ctypes.data, len(pos), stream), "hc_world_unload")
+
+    def set_cluster(self, ctas_per_chunk: int):
+        """CTAs (SMs) that mesh one chunk together in remesh: 1, 2, 4 or 8."""
+        self.ctx.check(self.lib.hc_world_set_cluster(self.handle, ctas_per_chunk), "hc_world_set_cluster")
 
     def touch(self, stream=None):
         """Rebuilds every resident chunk's light planes (after writing the pool directly)."""

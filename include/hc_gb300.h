@@ -215,6 +215,9 @@ hc_status hc_world_load(hc_world *world, const hc_chunk_load *loads, uint32_t n,
 /* Takes `n` chunks (positions: host int32 x 3n) out of the world; their slots are free once the
  * stream passes this point. A pending remesh of them is dropped (ChunkTaskData<kMesh>::OnUnload). */
 hc_status hc_world_unload(hc_world *world, const int32_t *positions, uint32_t n, void *stream);
+/* How many CTAs (SMs) mesh one chunk together in hc_world_remesh: 1, 2, 4 (default) or 8. More
+ * finish a pass of few heavy chunks sooner; 1 gives the most chunks per second on large passes. */
+hc_status hc_world_set_cluster(hc_world *world, int ctas_per_chunk);
 /* Rebuilds the per-chunk light planes of every resident chunk before the next remesh: call after
  * writing resident chunks' pool data by other means (hc_pool_upload). Synchronous. */
 hc_status hc_world_touch(hc_world *world, void *stream);
@@ -251,7 +254,7 @@ typedef struct hc_server_config {
 	uint32_t max_loads_per_tick; /* loads + unloads per tick */
 	uint64_t arena_quads;        /* per pass in flight; a chunk that does not fit is remeshed by a later pass */
 	uint32_t arena_meshes;
-	uint32_t reserved;
+	uint32_t ctas_per_chunk;     /* SMs meshing one chunk together (hc_world_set_cluster); 0: 4 */
 } hc_server_config;
 
 enum { HC_REQ_EDIT = 0, HC_REQ_FILL = 1, HC_REQ_LOAD = 2, HC_REQ_UNLOAD = 3 };
@@ -330,9 +333,9 @@ hc_status hc_server_replay(hc_server *server, const hc_request *requests, const 
  * held until exit). It calls no cudaMalloc, cudaFree or other allocating routine.
  *
  * Limit: 1..HC_NOALLOC_MAX_CHUNKS chunks per call; larger batches return HC_ERR_CAPACITY.
- * The first call on a device (the current one) sets the tables up with synchronous copies: make it
- * before any stream capture. All calls on a device share the scratch, so calls that overlap on the
- * GPU race; run them in one stream or one at a time. Synchronous: it waits for its stream.
+ * The first call on a device (the current one) sets the tables up with synchronous copies. All
+ * calls on a device share the scratch, so calls that overlap on the GPU race; run them in one
+ * stream or one at a time. Synchronous: it waits for its stream.
  * results_host (n x 5 words, may be NULL) receives {opaque quads, transparent quads, first mesh,
  * mesh count, status} per chunk; error_text (may be NULL) receives a message.
  * ---------------------------------------------------------------------------------------------- */

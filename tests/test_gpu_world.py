@@ -12,7 +12,7 @@ def _meshes_of_chunk(oracle, w, cell):
     return oracle.mesh_chunk([w.blocks[k] for k in nb], [w.heights[k] for k in nb])
 
 
-def _run(ctx, oracle, edits, world_factory):
+def _run(ctx, oracle, edits, world_factory, cluster=None):
     from hypercraft_gb300 import batch, world as hw
     from oracle import edits as oe
     w_gpu = world_factory()
@@ -21,6 +21,8 @@ def _run(ctx, oracle, edits, world_factory):
     dirty_ref = oe.apply_edits(w_ref, edits)
 
     rw = hw.ResidentWorld(ctx, w_gpu)
+    if cluster:
+        rw.set_cluster(cluster)
     rw.apply_edits(edits)
     arena = batch.Arena(4_000_000, 8192, w_gpu.n_chunks)
     cells, q, m = rw.remesh(arena)
@@ -48,9 +50,11 @@ def _run(ctx, oracle, edits, world_factory):
     return len(cells)
 
 
-def test_seeded_edits_match_reference_chain(ctx, oracle):
+@pytest.mark.parametrize("cluster", [1, 2, 4, 8])
+def test_seeded_edits_match_reference_chain(ctx, oracle, cluster):
+    """Every cluster size (CTAs meshing one chunk together) gives the reference's meshes."""
     from hypercraft_gb300 import world as hw
-    n = _run(ctx, oracle, hw.seeded_edits(4096, seed=7), hw.edit_world)
+    n = _run(ctx, oracle, hw.seeded_edits(4096, seed=7), hw.edit_world, cluster)
     assert n > 10
 
 
