@@ -29,9 +29,12 @@ constexpr int kLtCells = kLt * kLt * kLt; // 39,304
 constexpr int kWin = 62;
 constexpr int kWinRows = kWin * kWin; // 3,844
 // Per-chunk bit planes (pass, sun, level-15 emitters) as 32-bit rows (bit = x, row = z + 32 y),
-// plus a flag word (bit 0: the chunk holds an emitter of level 1..14).
+// plus one flag bit per row (the row holds an emitter of level 1..14), then the chunk's block
+// class ids, one byte per cell in the reference's cell order.
 constexpr int kPlaneWords = 1024;
-constexpr int kPlaneStride = 3 * kPlaneWords + 32;
+constexpr int kPlaneClassOff = 3 * kPlaneWords + 32;     // words
+constexpr int kPlaneBits = kPlaneClassOff;                // the bit planes alone
+constexpr int kPlaneStride = kPlaneClassOff + 32768 / 4; // 45,184 bytes per chunk
 enum { kPlanePass = 0, kPlaneSun = 1, kPlaneT15 = 2 };
 // Quad records staged for dense emission (two words each).
 constexpr int kQuadBuf = 4096;
@@ -143,6 +146,11 @@ __device__ __forceinline__ int nb_index(int x, int y, int z) {
 }
 __device__ __forceinline__ uint16_t raw_at(const Smem &S, int x, int y, int z) {
 	return S.blk[nb_index(x, y, z)][(x & 31) + ((y & 31) * kChunk + (z & 31)) * kChunk];
+}
+// Class id of a cell from the chunk planes (S.pln set for all 27 chunks).
+__device__ __forceinline__ uint8_t class_byte(const Smem &S, int x, int y, int z) {
+	const uint8_t *c = reinterpret_cast<const uint8_t *>(S.pln[nb_index(x, y, z)] + kPlaneClassOff);
+	return __ldg(c + (x & 31) + ((y & 31) * kChunk + (z & 31)) * kChunk);
 }
 // Chunk::GetSunlight: unsigned local y >= the int8 height converted to unsigned (Chunk.hpp:74-76).
 __device__ __forceinline__ bool sunlit(const Smem &S, int x, int y, int z) {

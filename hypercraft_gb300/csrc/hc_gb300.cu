@@ -132,18 +132,22 @@ __device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
 	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// Prefetches what the next chunk of a batch reads first: its own blocks and the 27 chunks' planes.
+// Prefetches what the next chunk of a batch reads first: its own class ids (or blocks) and the 27
+// chunks' bit planes.
 __device__ __forceinline__ void prefetch_item(const uint16_t *pool_blocks, const uint32_t *pool_planes, uint32_t pool_cap,
                                               const int32_t *nbr, uint32_t item) {
 	const int t = threadIdx.x;
 	if (t < 27) {
 		const int32_t slot = nbr[(size_t)item * 27 + t];
 		if (slot >= 0 && (uint32_t)slot < pool_cap) {
-			if (pool_planes)
-				prefetch_l2(pool_planes + (size_t)slot * kPlaneStride, kPlaneStride * sizeof(uint32_t));
-			if (t == 26)
+			if (pool_planes) {
+				prefetch_l2(pool_planes + (size_t)slot * kPlaneStride, kPlaneBits * sizeof(uint32_t));
+				if (t == 26)
+					prefetch_l2(pool_planes + (size_t)slot * kPlaneStride + kPlaneClassOff, 32768);
+			} else if (t == 26) {
 				for (int q = 0; q < 4; ++q)
 					prefetch_l2(pool_blocks + (size_t)slot * 32768 + q * 8192, 16384);
+			}
 		}
 	}
 }
@@ -801,9 +805,8 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 	if (p->d_light) {
 		const LightPass L{p->d_slots,  p->d_nb6,   p->pool->d_planes, p->pool->d_blocks,
 		                  p->d_levels, p->d_edges, p->d_light,        p->n_slots};
-		const int blocks = (int)std::min<uint64_t>(2ull * p->n_slots, (uint64_t)p->grid * 32);
 		for (int t = kLevels; t >= 1; --t) {
-			k_light_level<<<blocks, kLightThreads, 0, st>>>(L, tables(ctx), t);
+			k_light_level<<<p->n_slots, kLightThreads, 0, st>>>(L, tables(ctx), t);
 			HC_CUDA(ctx, cudaGetLastError());
 		}
 	}

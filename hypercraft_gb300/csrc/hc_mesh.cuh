@@ -41,8 +41,40 @@ struct Emit {
 	uint32_t qo;           // opaque quads (the transparent stream starts after them)
 };
 
-__device__ __forceinline__ void put_quad(Smem &S, const Emit &E, int st, uint32_t k, uint32_t g, const uint2 v[4], bool flip,
-                                         const uint32_t mn[3], const uint32_t mx[3]) {
+// Grows the bounding box of mesh (st, m) by [mn, mx]; one thread.
+__device__ __forceinline__ void aabb_add(Smem &S, int st, uint32_t m, const uint32_t mn[3], const uint32_t mx[3]) {
+	uint32_t *bb = S.aabb[st][m];
+	atomicMin(bb + 0, mn[0]), atomicMin(bb + 1, mn[1]), atomicMin(bb + 2, mn[2]);
+	atomicMax(bb + 3, mx[0]), atomicMax(bb + 4, mx[1]), atomicMax(bb + 5, mx[2]);
+}
+
+// The same for the quads of a whole warp (all lanes call it; `valid` lanes carry a quad): the quads
+// of the first valid lane's mesh are reduced over the full warp first, so a mesh's box takes six
+// atomics per warp instead of six per quad; lanes of another mesh add theirs one by one.
+__device__ __forceinline__ void aabb_add_warp(Smem &S, bool valid, int st, uint32_t m, const uint32_t mn[3],
+                                              const uint32_t mx[3]) {
+	const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+	if (!vmask)
+		return;
+	const int leader = __ffs(vmask) - 1;
+	const uint32_t key = ((uint32_t)st << 16) | m;
+	const uint32_t lkey = __shfl_sync(0xffffffffu, key, leader);
+	const bool same = valid && key == lkey;
+	uint32_t r[6];
+#pragma unroll
+	for (int c = 0; c < 3; ++c) {
+		r[c] = __reduce_min_sync(0xffffffffu, same ? mn[c] : 0xffffffffu);
+		r[3 + c] = __reduce_max_sync(0xffffffffu, same ? mx[c] : 0u);
+	}
+	if ((int)(threadIdx.x & 31) == leader)
+		aabb_add(S, (int)(lkey >> 16), lkey & 0xffffu, r, r + 3);
+	if (valid && !same)
+		aabb_add(S, st, m, mn, mx);
+}
+
+// Writes quad k of stream st (all-stream index g): 4 vertices, 6 indices, and the trigger of the
+// mesh it closes. The caller grows the mesh's box.
+__device__ __forceinline__ void put_quad(Smem &S, const Emit &E, int st, uint32_t k, uint32_t g, const uint2 v[4], bool flip) {
 	const unsigned long long q = E.q0 + (st ? E.qo : 0u) + k;
 	uint4 *vp = reinterpret_cast<uint4 *>(E.verts + 4 * q);
 	vp[0] = make_uint4(v[0].x, v[0].y, v[1].x, v[1].y);
@@ -61,9 +93,6 @@ __device__ __forceinline__ void put_quad(Smem &S, const Emit &E, int st, uint32_
 		ip[1] = (b + 3) | (b << 16);
 		ip[2] = (b + 1) | ((b + 3) << 16);
 	}
-	uint32_t *bb = S.aabb[st][m];
-	atomicMin(bb + 0, mn[0]), atomicMin(bb + 1, mn[1]), atomicMin(bb + 2, mn[2]);
-	atomicMax(bb + 3, mx[0]), atomicMax(bb + 4, mx[1]), atomicMax(bb + 5, mx[2]);
 	if (k > 0 && r == 0)
 		S.trig[st][m - 1] = g;
 }
@@ -83,18 +112,27 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 	static_assert(kRows % kBatch == 0, "row batches");
 	bool content = false, open = false;
 	for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
-		uint16_t raw[kBatch], rawe[kBatch];
-#pragma unroll
-		for (int j = 0; j < kBatch; ++j) {
-			const int y = (row0 + j) / kCls - 1, z = (row0 + j) % kCls - 1;
-			raw[j] = raw_at(S, lane, y, z);
-			rawe[j] = lane < 2 ? raw_at(S, lane ? kChunk : -1, y, z) : (uint16_t)0;
-		}
 		uint8_t c[kBatch], ce[kBatch];
+		if (S.pln[26]) { // class ids precomputed with the planes
 #pragma unroll
-		for (int j = 0; j < kBatch; ++j) {
-			c[j] = __ldg(T.class_of + raw[j]);
-			ce[j] = __ldg(T.class_of + rawe[j]);
+			for (int j = 0; j < kBatch; ++j) {
+				const int y = (row0 + j) / kCls - 1, z = (row0 + j) % kCls - 1;
+				c[j] = class_byte(S, lane, y, z);
+				ce[j] = lane < 2 ? class_byte(S, lane ? kChunk : -1, y, z) : (uint8_t)0;
+			}
+		} else {
+			uint16_t raw[kBatch], rawe[kBatch];
+#pragma unroll
+			for (int j = 0; j < kBatch; ++j) {
+				const int y = (row0 + j) / kCls - 1, z = (row0 + j) % kCls - 1;
+				raw[j] = raw_at(S, lane, y, z);
+				rawe[j] = lane < 2 ? raw_at(S, lane ? kChunk : -1, y, z) : (uint16_t)0;
+			}
+#pragma unroll
+			for (int j = 0; j < kBatch; ++j) {
+				c[j] = __ldg(T.class_of + raw[j]);
+				ce[j] = __ldg(T.class_of + rawe[j]);
+			}
 		}
 #pragma unroll
 		for (int j = 0; j < kBatch; ++j) {
@@ -235,7 +273,9 @@ __device__ void custom_emit(Smem &S, const Emit &E, int first, uint32_t ko, uint
 				v[c] = pack_vertex(p[0], p[1], p[2], mf.axis, mf.render_face, ao & 0xffu, sun & 0xffu, torch & 0xffu,
 				                   mf.texture);
 			}
-			put_quad(S, E, st, st ? kt : ko, g, v, true, mn, mx);
+			const uint32_t kq = st ? kt : ko;
+			put_quad(S, E, st, kq, g, v, true);
+			aabb_add(S, st, kq / kQuadsPerMesh, mn, mx);
 			if (st)
 				++kt;
 			else
@@ -532,84 +572,76 @@ __device__ void planes_count(Smem &S, const Split &sp) {
 	}
 }
 
-// Writes quad (u, v, w, h) of plane p: stream st, stream index k, all-stream index g.
-__device__ void emit_plane_quad(Smem &S, const Emit &E, int p, int u, int v, int w, int h, int st, uint32_t k, uint32_t g) {
-	const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
-	const bool uv_cycle = a != 2; // (U + 1) % 3 == V for the YZX swizzle (BlockMeshAlgo.hpp:384)
-	uint16_t t;
-	Light4 l;
-	face_key(S, a, s, inv, u, v, &t, &l);
-	int o[3], hv[3], wv[3];
-	to_xyz(a, s, u, v, o[0], o[1], o[2]);
-	to_xyz(a, 0, h, 0, hv[0], hv[1], hv[2]);
-	to_xyz(a, 0, 0, w, wv[0], wv[1], wv[2]);
-	const bool hfirst = (inv != 0) != uv_cycle;
-	const int *du = hfirst ? hv : wv, *dv = hfirst ? wv : hv;
-	const uint32_t face = (uint32_t)(2 * a + inv);
-	uint2 vt[4];
-	const int cx[4] = {o[0], o[0] + du[0], o[0] + du[0] + dv[0], o[0] + dv[0]};
-	const int cy[4] = {o[1], o[1] + du[1], o[1] + du[1] + dv[1], o[1] + dv[1]};
-	const int cz[4] = {o[2], o[2] + du[2], o[2] + du[2] + dv[2], o[2] + dv[2]};
+// Writes quad (u, v, w, h) of plane p: stream st, stream index k, all-stream index g. Called by all
+// lanes of a warp; lanes without a quad (valid false) only take part in the box reduction.
+__device__ void emit_plane_quad(Smem &S, const Emit &E, bool valid, int p, int u, int v, int w, int h, int st, uint32_t k,
+                                uint32_t g) {
+	uint32_t mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+	if (valid) {
+		const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
+		const bool uv_cycle = a != 2; // (U + 1) % 3 == V for the YZX swizzle (BlockMeshAlgo.hpp:384)
+		uint16_t t;
+		Light4 l;
+		face_key(S, a, s, inv, u, v, &t, &l);
+		int o[3], hv[3], wv[3];
+		to_xyz(a, s, u, v, o[0], o[1], o[2]);
+		to_xyz(a, 0, h, 0, hv[0], hv[1], hv[2]);
+		to_xyz(a, 0, 0, w, wv[0], wv[1], wv[2]);
+		const bool hfirst = (inv != 0) != uv_cycle;
+		const int *du = hfirst ? hv : wv, *dv = hfirst ? wv : hv;
+		const uint32_t face = (uint32_t)(2 * a + inv);
+		uint2 vt[4];
+		const int cx[4] = {o[0], o[0] + du[0], o[0] + du[0] + dv[0], o[0] + dv[0]};
+		const int cy[4] = {o[1], o[1] + du[1], o[1] + du[1] + dv[1], o[1] + dv[1]};
+		const int cz[4] = {o[2], o[2] + du[2], o[2] + du[2] + dv[2], o[2] + dv[2]};
 #pragma unroll
-	for (int c = 0; c < 4; ++c)
-		vt[c] = pack_vertex((uint32_t)cx[c] << 4, (uint32_t)cy[c] << 4, (uint32_t)cz[c] << 4, (uint32_t)a, face,
-		                    ao_get(l.ao, c), l4_get(l.sun, c), l4_get(l.torch, c), t);
-	const uint32_t mn[3] = {(uint32_t)cx[0] << 4, (uint32_t)cy[0] << 4, (uint32_t)cz[0] << 4};
-	const uint32_t mx[3] = {(uint32_t)cx[2] << 4, (uint32_t)cy[2] << 4, (uint32_t)cz[2] << 4};
-	put_quad(S, E, st, k, g, vt, flip_of(l), mn, mx);
+		for (int c = 0; c < 4; ++c)
+			vt[c] = pack_vertex((uint32_t)cx[c] << 4, (uint32_t)cy[c] << 4, (uint32_t)cz[c] << 4, (uint32_t)a, face,
+			                    ao_get(l.ao, c), l4_get(l.sun, c), l4_get(l.torch, c), t);
+		mn[0] = (uint32_t)cx[0] << 4, mn[1] = (uint32_t)cy[0] << 4, mn[2] = (uint32_t)cz[0] << 4;
+		mx[0] = (uint32_t)cx[2] << 4, mx[1] = (uint32_t)cy[2] << 4, mx[2] = (uint32_t)cz[2] << 4;
+		put_quad(S, E, st, k, g, vt, flip_of(l));
+	}
+	aabb_add_warp(S, valid, st, k / kQuadsPerMesh, mn, mx);
 }
 
-__device__ __forceinline__ void emit_record(Smem &S, const Emit &E, uint2 r) {
+__device__ __forceinline__ void emit_record(Smem &S, const Emit &E, bool valid, uint2 r) {
 	const int p = (int)(r.x & 255u), st = (int)((r.x >> 28) & 1u);
 	const uint32_t li = r.y & 0xffffu, lk = r.y >> 16;
-	emit_plane_quad(S, E, p, (int)((r.x >> 8) & 31u), (int)((r.x >> 13) & 31u), (int)((r.x >> 18) & 31u) + 1,
-	                (int)((r.x >> 23) & 31u) + 1, st, S.seg_base[st][1 + p] + lk, S.seg_base[2][1 + p] + li);
+	emit_plane_quad(S, E, valid, p, (int)((r.x >> 8) & 31u), (int)((r.x >> 13) & 31u), (int)((r.x >> 18) & 31u) + 1,
+	                (int)((r.x >> 23) & 31u) + 1, st, valid ? S.seg_base[st][1 + p] + lk : 0u,
+	                valid ? S.seg_base[2][1 + p] + li : 0u);
 }
 
-// Emits the plane quads. Normally planes_count kept all their records; otherwise the quads are
-// taken in windows of kQuadBuf (in output order), the planes overlapping a window re-run their
-// merge to stage that window's records, and the CTA writes them.
-__device__ void planes_emit(Smem &S, const Emit &E, uint32_t custom_all, uint32_t plane_quads, const Split &sp) {
+// Emits the plane quads this CTA owns. Normally planes_count kept all their records and every
+// thread writes some; otherwise each warp merges its planes again and writes their quads as it
+// finds them (a plane's quads go to its segment base plus their index in the plane).
+__device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	if (!S.misc[5]) {
-		for (uint32_t j = tid; j < S.misc[4]; j += kThreads)
-			emit_record(S, E, S.aux.quads[j]);
+		const uint32_t n = S.misc[4];
+		for (uint32_t j0 = (uint32_t)warp * 32; j0 < n; j0 += kThreads) {
+			const uint32_t j = j0 + lane;
+			emit_record(S, E, j < n, j < n ? S.aux.quads[j] : make_uint2(0, 0));
+		}
 		return;
 	}
 	const uint32_t lt = (1u << lane) - 1u;
-	for (uint32_t w0 = 0; w0 < plane_quads; w0 += kQuadBuf) {
-		if (sp.c > 1) { // other CTAs' quads of this window stay unfilled here
-			for (int j = tid; j < kQuadBuf; j += kThreads)
-				S.aux.quads[j].x = 0xffffffffu;
-			__syncthreads();
-		}
-		for (int j = warp; j < sp.planes(); j += kWarps) {
-			const int p = sp.plane(j);
-			const uint32_t pb = S.seg_base[2][1 + p] - custom_all;
-			const uint32_t pc = S.seg_cnt[0][1 + p] + S.seg_cnt[1][1 + p];
-			if (!pc || pb >= w0 + kQuadBuf || pb + pc <= w0)
-				continue;
-			uint32_t n_all = 0, n_st[2] = {0, 0};
-			warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
-				if (is_start) {
-					const int st = (int)((tmask >> lane) & 1u);
-					const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
-					const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
-					const uint32_t i = pb + li;
-					if (i >= w0 && i < w0 + kQuadBuf)
-						S.aux.quads[i - w0] = quad_record(p, u, lane, w, h, st, li, lk);
-				}
-				n_all += __popc(starts);
-				n_st[1] += __popc(starts & tmask);
-				n_st[0] += __popc(starts & ~tmask);
-			});
-		}
-		__syncthreads();
-		const uint32_t n = min((uint32_t)kQuadBuf, plane_quads - w0);
-		for (uint32_t j = tid; j < n; j += kThreads)
-			if (S.aux.quads[j].x != 0xffffffffu)
-				emit_record(S, E, S.aux.quads[j]);
-		__syncthreads();
+	for (int jp = warp; jp < sp.planes(); jp += kWarps) {
+		const int p = sp.plane(jp);
+		if (!(S.seg_cnt[0][1 + p] + S.seg_cnt[1][1 + p]))
+			continue;
+		const uint32_t bk[2] = {S.seg_base[0][1 + p], S.seg_base[1][1 + p]}, bg = S.seg_base[2][1 + p];
+		uint32_t n_all = 0, n_st[2] = {0, 0};
+		warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
+			const int st = (int)((tmask >> lane) & 1u);
+			const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
+			const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
+			emit_plane_quad(S, E, is_start, p, u, lane, w, h, st, bk[st] + lk, bg + li);
+			n_all += __popc(starts);
+			n_st[1] += __popc(starts & tmask);
+			n_st[0] += __popc(starts & ~tmask);
+		});
 	}
 }
 
@@ -790,12 +822,11 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 	const Emit E{A.verts, A.idx, q0, qo};
 	if (lead)
 		custom_emit(S, E, tid * kBlocksPerThread, eo, et, eo + et);
-	const uint32_t custom_all = S.seg_base[2][1];
-	planes_emit(S, E, custom_all, q - custom_all, sp);
+	planes_emit(S, E, sp);
+	__syncthreads(); // every quad's box and closing position is in before the descriptors are written
 
 	if (sp.c > 1) { // CTA 0 merges the boxes and closing positions of every CTA's quads
 		cg::cluster_group cl = cg::this_cluster();
-		__syncthreads();
 		cl.sync();
 		if (lead)
 			for (int i = tid; i < 2 * kMaxMeshesPerStream; i += kThreads) {

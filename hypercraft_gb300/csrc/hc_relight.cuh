@@ -234,7 +234,7 @@ __device__ void relight_window(Smem &S, const DevTables &T) {
 // level 1..14. Uniform rows (one raw value) take one lookup.
 __device__ __forceinline__ bool chunk_plane_row(const uint16_t *blk, const int8_t *hgt, const DevClass *classes,
                                                 const uint8_t *class_of, int y, int z, uint32_t &pass, uint32_t &sun,
-                                                uint32_t &t15) {
+                                                uint32_t &t15, uint32_t cls[8]) {
 	const uint4 *row = reinterpret_cast<const uint4 *>(blk + (y * kChunk + z) * kChunk);
 	uint4 q[4];
 #pragma unroll
@@ -248,22 +248,31 @@ __device__ __forceinline__ bool chunk_plane_row(const uint16_t *blk, const int8_
 	bool low = false;
 	pass = t15 = 0;
 	if (uniform) {
-		const DevClass &k = classes[__ldg(class_of + (w0 & 0xffffu))];
+		const uint32_t c = __ldg(class_of + (w0 & 0xffffu));
+		const DevClass &k = classes[c];
 		pass = (k.flags & kFIndirect) ? 0xffffffffu : 0u;
 		t15 = k.light >= 15 ? 0xffffffffu : 0u;
 		low = k.light > 0 && k.light < 15;
+#pragma unroll
+		for (int i = 0; i < 8; ++i)
+			cls[i] = c * 0x01010101u;
 	} else {
+#pragma unroll
+		for (int i = 0; i < 8; ++i)
+			cls[i] = 0;
 #pragma unroll
 		for (int i = 0; i < 4; ++i) {
 			const uint32_t ws[4] = {q[i].x, q[i].y, q[i].z, q[i].w};
 #pragma unroll
 			for (int j = 0; j < 8; ++j) {
 				const uint32_t raw = (ws[j >> 1] >> (16 * (j & 1))) & 0xffffu;
-				const DevClass &k = classes[__ldg(class_of + raw)];
+				const uint32_t c = __ldg(class_of + raw);
+				const DevClass &k = classes[c];
 				const int x = 8 * i + j;
 				pass |= (uint32_t)((k.flags & kFIndirect) != 0) << x;
 				t15 |= (uint32_t)(k.light >= 15) << x;
 				low |= k.light > 0 && k.light < 15;
+				cls[x >> 2] |= c << (8 * (x & 3));
 			}
 		}
 	}
@@ -282,11 +291,14 @@ __device__ __forceinline__ bool chunk_plane_row(const uint16_t *blk, const int8_
 // Bit planes of chunks: one thread per 32-cell row, 32 rows (one flag word) per warp.
 __device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hgt, const DevClass *cls_smem,
                                            const uint8_t *class_of, int r, uint32_t *out) {
-	uint32_t pass, sun, t15;
-	const bool low = chunk_plane_row(blk, hgt, cls_smem, class_of, r >> 5, r & 31, pass, sun, t15);
+	uint32_t pass, sun, t15, cls[8];
+	const bool low = chunk_plane_row(blk, hgt, cls_smem, class_of, r >> 5, r & 31, pass, sun, t15, cls);
 	out[kPlanePass * kPlaneWords + r] = pass;
 	out[kPlaneSun * kPlaneWords + r] = sun;
 	out[kPlaneT15 * kPlaneWords + r] = t15;
+	uint4 *co = reinterpret_cast<uint4 *>(out + kPlaneClassOff + 8 * r);
+	co[0] = make_uint4(cls[0], cls[1], cls[2], cls[3]);
+	co[1] = make_uint4(cls[4], cls[5], cls[6], cls[7]);
 	const uint32_t lows = __ballot_sync(0xffffffffu, low);
 	if ((threadIdx.x & 31) == 0)
 		out[3 * kPlaneWords + (r >> 5)] = lows;
@@ -309,7 +321,8 @@ __device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hg
 constexpr int kLevels = 15;
 constexpr size_t kLevelSlotWords = (size_t)2 * kLevels * kPlaneWords; // per chunk: 2 channels x 15 levels
 constexpr size_t kEdgeSlotWords = (size_t)2 * kLevels * 2 * 32;       // per chunk: x = 0 and x = 31 bits
-constexpr int kLightThreads = 512;                                     // two blocks per chunk
+constexpr int kLightThreads = 256;                                     // one block per chunk
+constexpr int kLightRows = kPlaneWords / kLightThreads;                // rows per thread
 
 struct LightPass {
 	const int32_t *slots;   // batch chunk -> pool slot
@@ -340,73 +353,110 @@ __device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
 	           mux(b[2], mux(b[1], s[6], s[4]), mux(b[1], s[2], s[0])));
 }
 
-// Level t of every batch chunk: a block of kLightThreads rows (half a chunk), one row per thread,
-// both channels, every load independent; also the row edge bits the x neighbours read at the next
-// level. Level 1 also writes the cells' light bytes.
+// Level t of every batch chunk, one block per chunk: the chunk's level t + 1 rows and the rows and
+// edge bits of its six face neighbours that touch it are staged in shared memory with coalesced
+// loads, then each thread dilates kLightRows rows of both channels. Also writes the row edge bits
+// that the x neighbours read at the next level. Level 1 also writes the cells' light bytes.
 __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevTables T, int t) {
+	__shared__ __align__(16) uint32_t prev[2][kPlaneWords];
+	__shared__ uint32_t side[2][6][32]; // per channel: -x hi edge, +x lo edge, -y rows, +y rows, -z rows, +z rows
 	__shared__ int s_nb[6];
 	__shared__ int32_t s_slot;
 	const int tid = threadIdx.x, lane = tid & 31;
-	for (uint32_t blk = blockIdx.x; blk < 2 * L.n; blk += gridDim.x) {
-		const int i = (int)(blk >> 1), r = (int)(blk & 1u) * kLightThreads + tid, y = r >> 5, z = r & 31;
-		if (tid < 6)
-			s_nb[tid] = __ldg(L.nb6 + 6 * i + tid);
-		if (tid == 6)
-			s_slot = __ldg(L.slots + i);
-		__syncthreads();
-		const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
-		uint32_t s[2];
-		if (t == kLevels) {
-			s[0] = __ldg(P + kPlaneSun * kPlaneWords + r);
-			s[1] = __ldg(P + kPlaneT15 * kPlaneWords + r);
-		} else {
-			const int xm = s_nb[0], xp = s_nb[1];
-			const int yi = y > 0 ? i : s_nb[2], yr = y > 0 ? r - 32 : r + 31 * 32;
-			const int yj = y < 31 ? i : s_nb[3], yq = y < 31 ? r + 32 : r - 31 * 32;
-			const int zi = z > 0 ? i : s_nb[4], zr = z > 0 ? r - 1 : r + 31;
-			const int zj = z < 31 ? i : s_nb[5], zq = z < 31 ? r + 1 : r - 31;
-			const uint32_t pass = __ldg(P + kPlanePass * kPlaneWords + r);
-			uint32_t v[2][7];
+	const int i = blockIdx.x;
+	if (tid < 6)
+		s_nb[tid] = __ldg(L.nb6 + 6 * i + tid);
+	if (tid == 6)
+		s_slot = __ldg(L.slots + i);
+	__syncthreads();
+	const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
+	if (t < kLevels) {
 #pragma unroll
-			for (int c = 0; c < 2; ++c) {
-				v[c][0] = __ldg(level_plane(L, i, c, t + 1) + r);
-				v[c][1] = xm >= 0 ? __ldg(level_edges(L, xm, c, t + 1) + 32 + (r >> 5)) : 0u;
-				v[c][2] = xp >= 0 ? __ldg(level_edges(L, xp, c, t + 1) + (r >> 5)) : 0u;
-				v[c][3] = yi >= 0 ? __ldg(level_plane(L, yi, c, t + 1) + yr) : 0u;
-				v[c][4] = yj >= 0 ? __ldg(level_plane(L, yj, c, t + 1) + yq) : 0u;
-				v[c][5] = zi >= 0 ? __ldg(level_plane(L, zi, c, t + 1) + zr) : 0u;
-				v[c][6] = zj >= 0 ? __ldg(level_plane(L, zj, c, t + 1) + zq) : 0u;
+		for (int c = 0; c < 2; ++c) {
+			const uint4 *src = reinterpret_cast<const uint4 *>(level_plane(L, i, c, t + 1));
+			uint4 *dst = reinterpret_cast<uint4 *>(prev[c]);
+			for (int j = tid; j < kPlaneWords / 4; j += kLightThreads)
+				dst[j] = __ldg(src + j);
+		}
+		for (int j = tid; j < 2 * 6 * 32; j += kLightThreads) {
+			const int c = j / 192, f = (j / 32) % 6, k = j & 31, nb = s_nb[f];
+			uint32_t v = 0;
+			if (nb >= 0) {
+				if (f == 0)
+					v = __ldg(level_edges(L, nb, c, t + 1) + 32 + k); // x = 31 bits of the -x neighbour
+				else if (f == 1)
+					v = __ldg(level_edges(L, nb, c, t + 1) + k); // x = 0 bits of the +x neighbour
+				else if (f == 2)
+					v = __ldg(level_plane(L, nb, c, t + 1) + 31 * 32 + k); // its y = 31 row at z = k
+				else if (f == 3)
+					v = __ldg(level_plane(L, nb, c, t + 1) + k); // y = 0, z = k
+				else if (f == 4)
+					v = __ldg(level_plane(L, nb, c, t + 1) + k * 32 + 31); // z = 31 row at y = k
+				else
+					v = __ldg(level_plane(L, nb, c, t + 1) + k * 32); // z = 0, y = k
 			}
+			side[c][f][k] = v;
+		}
+	}
+	uint32_t pass[kLightRows], lows[kLightRows], s[kLightRows][2];
+#pragma unroll
+	for (int k = 0; k < kLightRows; ++k) {
+		const int r = tid + k * kLightThreads;
+		pass[k] = __ldg(P + kPlanePass * kPlaneWords + r);
+		lows[k] = __ldg(P + 3 * kPlaneWords + (r >> 5));
+		if (t == kLevels) {
+			s[k][0] = __ldg(P + kPlaneSun * kPlaneWords + r);
+			s[k][1] = __ldg(P + kPlaneT15 * kPlaneWords + r);
+		}
+	}
+	__syncthreads();
+	if (t < kLevels) {
+#pragma unroll
+		for (int k = 0; k < kLightRows; ++k) {
+			const int r = tid + k * kLightThreads, y = r >> 5, z = r & 31;
 #pragma unroll
 			for (int c = 0; c < 2; ++c) {
-				const uint32_t prev = v[c][0];
-				const uint32_t d = (prev << 1) | (prev >> 1) | ((v[c][1] >> (r & 31)) & 1u) |
-				                   (((v[c][2] >> (r & 31)) & 1u) << 31) | v[c][3] | v[c][4] | v[c][5] | v[c][6];
-				s[c] = prev | (pass & d);
+				const uint32_t me = prev[c][r];
+				uint32_t d = (me << 1) | (me >> 1);
+				d |= (side[c][0][r >> 5] >> (r & 31)) & 1u;
+				d |= ((side[c][1][r >> 5] >> (r & 31)) & 1u) << 31;
+				d |= y > 0 ? prev[c][r - 32] : side[c][2][z];
+				d |= y < 31 ? prev[c][r + 32] : side[c][3][z];
+				d |= z > 0 ? prev[c][r - 1] : side[c][4][y];
+				d |= z < 31 ? prev[c][r + 1] : side[c][5][y];
+				s[k][c] = me | (pass[k] & d);
 			}
 		}
-		if ((__ldg(P + 3 * kPlaneWords + (r >> 5)) >> (r & 31)) & 1u) { // emitters below level 15 in this row
+	}
+#pragma unroll
+	for (int k = 0; k < kLightRows; ++k) {
+		const int r = tid + k * kLightThreads;
+		if ((lows[k] >> (r & 31)) & 1u) { // emitters below level 15 in this row
 			const uint16_t *row = L.blocks + (size_t)s_slot * 32768 + r * 32;
 			for (int x = 0; x < 32; ++x)
 				if (T.classes[T.class_of[row[x]]].light >= t)
-					s[1] |= 1u << x;
+					s[k][1] |= 1u << x;
 		}
 #pragma unroll
 		for (int c = 0; c < 2; ++c) {
 			uint32_t *out = L.levels + (size_t)i * kLevelSlotWords + (size_t)(c * kLevels + t - 1) * kPlaneWords;
-			out[r] = s[c];
-			const uint32_t lo = __ballot_sync(0xffffffffu, s[c] & 1u), hi = __ballot_sync(0xffffffffu, s[c] >> 31);
+			out[r] = s[k][c];
+			const uint32_t lo = __ballot_sync(0xffffffffu, s[k][c] & 1u), hi = __ballot_sync(0xffffffffu, s[k][c] >> 31);
 			if (lane == 0) {
 				uint32_t *e = L.edges + (size_t)i * kEdgeSlotWords + (size_t)(c * kLevels + t - 1) * 64;
 				e[r >> 5] = lo;
 				e[32 + (r >> 5)] = hi;
 			}
 		}
-		if (t == 1) {
+	}
+	if (t == 1) {
+#pragma unroll 1
+		for (int k = 0; k < kLightRows; ++k) {
+			const int r = tid + k * kLightThreads;
 			uint32_t lv[kLevels], b[2][4];
 #pragma unroll
 			for (int c = 0; c < 2; ++c) {
-				lv[0] = s[c];
+				lv[0] = s[k][c];
 #pragma unroll
 				for (int u = 2; u <= kLevels; ++u)
 					lv[u - 1] = __ldg(level_plane(L, i, c, u) + r);
@@ -417,13 +467,13 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 			for (int q = 0; q < 8; ++q) {
 				uint32_t val = 0;
 #pragma unroll
-				for (int k = 0; k < 4; ++k) {
-					const int x = 4 * q + k;
+				for (int kk = 0; kk < 4; ++kk) {
+					const int x = 4 * q + kk;
 					uint32_t byte = 0;
 #pragma unroll
 					for (int bit = 0; bit < 4; ++bit)
 						byte |= ((b[0][bit] >> x) & 1u) << bit | ((b[1][bit] >> x) & 1u) << (bit + 4);
-					val |= byte << (8 * k);
+					val |= byte << (8 * kk);
 				}
 				w[q] = val;
 			}
@@ -431,7 +481,6 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
 			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
 		}
-		__syncthreads(); // s_nb, s_slot are rewritten for the next block
 	}
 }
 
