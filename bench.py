@@ -40,6 +40,7 @@ def parse():
     ap.add_argument("--rates", default="2000,5000,10000,20000", help="serve: Poisson arrival rates (requests/s)")
     ap.add_argument("--seconds", type=float, default=3.0, help="serve: trace length per rate")
     ap.add_argument("--ctas", type=int, default=4, help="serve: CTAs meshing one chunk together (1, 2, 4, 8)")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="default line: serving trace length (0: skip)")
     ap.add_argument("--size", default="", help="override grid as NXxNYxNZ (profiling runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the per-chunk form (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -332,6 +333,16 @@ def ours(args):
                "h2d_bytes_per_step": int(w.n_chunks * (65536 + 1024)),
                "d2h_bytes_per_step": int(quads * 44 + meshes * DESC_BYTES + n * RESULT_BYTES)}
 
+    serving = None
+    if rank == 0 and world == 1 and args.serve_seconds > 0:
+        rows, _ = serve_rates(ctx, [10000.0], args.serve_seconds, args.ctas)
+        r = rows[0]
+        serving = {"workload": "serve: seeded trace at 10,000 requests/s (70% edits, 25% view loads along a "
+                               "random walk, 5% 16^3 fills), 1 ms ticks, pool sized by free HBM",
+                   "edit_p50_ms": r["edit_p50_ms"], "edit_p99_ms": r["edit_p99_ms"], "p50_ms": r["p50_ms"],
+                   "p99_ms": r["p99_ms"], "requests_per_s": r["requests_per_s"], "chunks_per_s": r["chunks_per_s"],
+                   "seconds": r["seconds"], "ctas_per_chunk": args.ctas}
+
     cpu = None
     if rank == 0 and world >= 1 and not args.no_cpu:
         from oracle import bind
@@ -361,7 +372,9 @@ def ours(args):
                          "frac": achieved / peak, "traffic": None,
                          "peak_source": f"{peak_kind} ({'MEASURED_PEAKS.json hbm_gbs' if peak_kind == 'measured' else 'fallback'})",
                          "algorithmic_bytes_per_launch": algo_bytes},
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+            "serving": serving,
+            # per step the plan's graph runs 18 kernels: planes, 15 light levels, light bytes, mesh
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * 18,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
@@ -428,29 +441,18 @@ def _pct(x, q):
     return float(np.percentile(x, q)) if len(x) else None
 
 
-def serve_bench(args):
-    """Serving workload: a device pool sized by free HBM (at most 65,536 chunks) over a 96 x 32 x 96
-    chunk grid; a player takes a seeded random walk and the chunks of a view sphere of radius 16
-    chunks around it are resident. Poisson arrivals at each rate: 70% single-block edits within
-    48 voxels of the player, 25% loads of chunks entering the view (mixture chunks: 30% air, 20%
-    stone, 35% terrain, 10% random fill, 5% checkerboard), 5% 16^3 region fills; unloads of the
-    chunks leaving the view go in before the loads. 1 ms ticks, three passes in flight. Latency =
-    arrival to completion of the request's pass; the initial view is loaded before timing."""
-    import torch
-    from hypercraft_gb300 import mesher, server as hs
-    from hypercraft_gb300.build import build
-    build()
-    ctx = mesher.Context(0)
+def serve_rates(ctx, rates, seconds, ctas):
+    """Replays the seeded serving trace at each rate on a fresh server; one result row per rate."""
+    from hypercraft_gb300 import server as hs
     lib = hs.ChunkLibrary(16, 8, 16, seed=0x5E7E)
-    rows = []
+    rows, clocks = [], None
     names = {hs.REQ_EDIT: "edit", hs.REQ_FILL: "fill", hs.REQ_LOAD: "load", hs.REQ_UNLOAD: "unload"}
-    clocks = None
-    for rate in [float(r) for r in args.rates.split(",")]:
+    for rate in rates:
         wl = hs.ServingWorkload(lib, seed=int(rate))
         init = wl.initial_loads()
-        reqs, times = wl.trace(rate, args.seconds)
+        reqs, times = wl.trace(rate, seconds)
         srv = hs.Server(ctx, wl.grid, wl.origin, pool_capacity=0, tick_us=1000, depth=3, max_edits_per_tick=16384,
-                        max_loads_per_tick=512, arena_quads=8 << 20, arena_meshes=1 << 16, ctas_per_chunk=args.ctas)
+                        max_loads_per_tick=512, arena_quads=8 << 20, arena_meshes=1 << 16, ctas_per_chunk=ctas)
         srv.submit(init)
         srv.drain()
         st0 = srv.stats()
@@ -480,6 +482,23 @@ def serve_bench(args):
             row[f"{name}_p99_ms"] = _pct(sel, 99)
         rows.append(row)
         srv.close()
+    return rows, clocks
+
+
+def serve_bench(args):
+    """Serving workload: a device pool sized by free HBM (at most 65,536 chunks) over a 96 x 32 x 96
+    chunk grid; a player takes a seeded random walk and the chunks of a view sphere of radius 16
+    chunks around it are resident. Poisson arrivals at each rate: 70% single-block edits within
+    48 voxels of the player, 25% loads of chunks entering the view (mixture chunks: 30% air, 20%
+    stone, 35% terrain, 10% random fill, 5% checkerboard), 5% 16^3 region fills; unloads of the
+    chunks leaving the view go in before the loads. 1 ms ticks, three passes in flight. Latency =
+    arrival to completion of the request's pass; the initial view is loaded before timing."""
+    from hypercraft_gb300 import mesher
+    from hypercraft_gb300.build import build
+    build()
+    ctx = mesher.Context(0)
+    rows, clocks = serve_rates(ctx, [float(r) for r in args.rates.split(",")], args.seconds, args.ctas)
+    for row in rows:
         print(json.dumps({"serve_rate": row}), flush=True)
     head = next((r for r in rows if r["rate"] == 10000.0), rows[-1])
     line = {"metric": "p99 single-edit relight+remesh latency at 10k requests/s", "value": head["edit_p99_ms"],

@@ -809,6 +809,9 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 			k_light_level<<<p->n_slots, kLightThreads, 0, st>>>(L, tables(ctx), t);
 			HC_CUDA(ctx, cudaGetLastError());
 		}
+		const uint64_t rows = (uint64_t)p->n_slots * kPlaneWords;
+		k_light_bytes<<<(int)std::min<uint64_t>((rows + 255) / 256, (uint64_t)p->grid * 16), 256, 0, st>>>(L);
+		HC_CUDA(ctx, cudaGetLastError());
 	}
 	const Arena A = plan_arena(p);
 	unsigned int *work = reinterpret_cast<unsigned int *>(p->d_state + 2);

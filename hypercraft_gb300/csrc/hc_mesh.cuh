@@ -108,15 +108,14 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 		S.classes[i] = T.classes[i];
 	__syncthreads();
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	constexpr int kRows = kCls * kCls, kBatch = 4; // 1156 rows = 289 batches
-	static_assert(kRows % kBatch == 0, "row batches");
+	constexpr int kRows = kCls * kCls, kBatch = 12; // 1156 rows; 12 in flight per warp
 	bool content = false, open = false;
 	for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
 		uint8_t c[kBatch], ce[kBatch];
 		if (S.pln[26]) { // class ids precomputed with the planes
 #pragma unroll
 			for (int j = 0; j < kBatch; ++j) {
-				const int y = (row0 + j) / kCls - 1, z = (row0 + j) % kCls - 1;
+				const int row = min(row0 + j, kRows - 1), y = row / kCls - 1, z = row % kCls - 1;
 				c[j] = class_byte(S, lane, y, z);
 				ce[j] = lane < 2 ? class_byte(S, lane ? kChunk : -1, y, z) : (uint8_t)0;
 			}
@@ -124,7 +123,7 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 			uint16_t raw[kBatch], rawe[kBatch];
 #pragma unroll
 			for (int j = 0; j < kBatch; ++j) {
-				const int y = (row0 + j) / kCls - 1, z = (row0 + j) % kCls - 1;
+				const int row = min(row0 + j, kRows - 1), y = row / kCls - 1, z = row % kCls - 1;
 				raw[j] = raw_at(S, lane, y, z);
 				rawe[j] = lane < 2 ? raw_at(S, lane ? kChunk : -1, y, z) : (uint16_t)0;
 			}
@@ -137,6 +136,8 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 #pragma unroll
 		for (int j = 0; j < kBatch; ++j) {
 			const int row = row0 + j, y = row / kCls - 1, z = row % kCls - 1;
+			if (row >= kRows) // the same for the whole warp
+				break;
 			uint16_t *dst = S.cell + row * kCls;
 			dst[lane + 1] = (uint16_t)(c[j] << 8);
 			if (lane < 2)
@@ -613,9 +614,10 @@ __device__ __forceinline__ void emit_record(Smem &S, const Emit &E, bool valid, 
 	                valid ? S.seg_base[2][1 + p] + li : 0u);
 }
 
-// Emits the plane quads this CTA owns. Normally planes_count kept all their records and every
-// thread writes some; otherwise each warp merges its planes again and writes their quads as it
-// finds them (a plane's quads go to its segment base plus their index in the plane).
+// Emits the plane quads this CTA owns. Normally planes_count kept all their records; otherwise
+// the quads are taken in windows of kQuadBuf (in output order), the planes overlapping a window
+// merge again to stage that window's records, and the whole CTA writes them. Emission of a window
+// is spread over every thread: a heavy plane does not wait on the warp that merges it.
 __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	if (!S.misc[5]) {
@@ -627,21 +629,43 @@ __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 		return;
 	}
 	const uint32_t lt = (1u << lane) - 1u;
-	for (int jp = warp; jp < sp.planes(); jp += kWarps) {
-		const int p = sp.plane(jp);
-		if (!(S.seg_cnt[0][1 + p] + S.seg_cnt[1][1 + p]))
-			continue;
-		const uint32_t bk[2] = {S.seg_base[0][1 + p], S.seg_base[1][1 + p]}, bg = S.seg_base[2][1 + p];
-		uint32_t n_all = 0, n_st[2] = {0, 0};
-		warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
-			const int st = (int)((tmask >> lane) & 1u);
-			const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
-			const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
-			emit_plane_quad(S, E, is_start, p, u, lane, w, h, st, bk[st] + lk, bg + li);
-			n_all += __popc(starts);
-			n_st[1] += __popc(starts & tmask);
-			n_st[0] += __popc(starts & ~tmask);
-		});
+	const uint32_t custom_all = S.seg_base[2][1];
+	const uint32_t plane_quads = S.misc[0] + S.misc[1] - custom_all;
+	for (uint32_t w0 = 0; w0 < plane_quads; w0 += kQuadBuf) {
+		if (sp.c > 1) { // other CTAs' quads of this window stay unfilled here
+			for (int j = tid; j < kQuadBuf; j += kThreads)
+				S.aux.quads[j].x = 0xffffffffu;
+			__syncthreads();
+		}
+		for (int jp = warp; jp < sp.planes(); jp += kWarps) {
+			const int p = sp.plane(jp);
+			const uint32_t pb = S.seg_base[2][1 + p] - custom_all;
+			const uint32_t pc = S.seg_cnt[0][1 + p] + S.seg_cnt[1][1 + p];
+			if (!pc || pb >= w0 + kQuadBuf || pb + pc <= w0)
+				continue;
+			uint32_t n_all = 0, n_st[2] = {0, 0};
+			warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
+				if (is_start) {
+					const int st = (int)((tmask >> lane) & 1u);
+					const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
+					const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
+					const uint32_t i = pb + li;
+					if (i >= w0 && i < w0 + kQuadBuf)
+						S.aux.quads[i - w0] = quad_record(p, u, lane, w, h, st, li, lk);
+				}
+				n_all += __popc(starts);
+				n_st[1] += __popc(starts & tmask);
+				n_st[0] += __popc(starts & ~tmask);
+			});
+		}
+		__syncthreads();
+		const uint32_t n = min((uint32_t)kQuadBuf, plane_quads - w0);
+		for (uint32_t j0 = (uint32_t)warp * 32; j0 < n; j0 += kThreads) {
+			const uint32_t j = j0 + lane;
+			const bool valid = j < n && S.aux.quads[j].x != 0xffffffffu;
+			emit_record(S, E, valid, valid ? S.aux.quads[j] : make_uint2(0, 0));
+		}
+		__syncthreads();
 	}
 }
 

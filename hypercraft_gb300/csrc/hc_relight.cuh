@@ -355,8 +355,9 @@ __device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
 
 // Level t of every batch chunk, one block per chunk: the chunk's level t + 1 rows and the rows and
 // edge bits of its six face neighbours that touch it are staged in shared memory with coalesced
-// loads, then each thread dilates kLightRows rows of both channels. Also writes the row edge bits
-// that the x neighbours read at the next level. Level 1 also writes the cells' light bytes.
+// loads (the chunk's own rows are requested before its neighbour list arrives), then each thread
+// dilates kLightRows rows of both channels. Also writes the row edge bits that the x neighbours
+// read at the next level.
 __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevTables T, int t) {
 	__shared__ __align__(16) uint32_t prev[2][kPlaneWords];
 	__shared__ uint32_t side[2][6][32]; // per channel: -x hi edge, +x lo edge, -y rows, +y rows, -z rows, +z rows
@@ -364,6 +365,15 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 	__shared__ int32_t s_slot;
 	const int tid = threadIdx.x, lane = tid & 31;
 	const int i = blockIdx.x;
+	constexpr int kQ = 2 * kPlaneWords / 4 / kLightThreads; // uint4 of the two channels per thread
+	uint4 own[kQ];
+	if (t < kLevels) {
+#pragma unroll
+		for (int q = 0; q < kQ; ++q) {
+			const int j = tid + q * kLightThreads, c = j / (kPlaneWords / 4), o = j % (kPlaneWords / 4);
+			own[q] = __ldg(reinterpret_cast<const uint4 *>(level_plane(L, i, c, t + 1)) + o);
+		}
+	}
 	if (tid < 6)
 		s_nb[tid] = __ldg(L.nb6 + 6 * i + tid);
 	if (tid == 6)
@@ -371,13 +381,6 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 	__syncthreads();
 	const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
 	if (t < kLevels) {
-#pragma unroll
-		for (int c = 0; c < 2; ++c) {
-			const uint4 *src = reinterpret_cast<const uint4 *>(level_plane(L, i, c, t + 1));
-			uint4 *dst = reinterpret_cast<uint4 *>(prev[c]);
-			for (int j = tid; j < kPlaneWords / 4; j += kLightThreads)
-				dst[j] = __ldg(src + j);
-		}
 		for (int j = tid; j < 2 * 6 * 32; j += kLightThreads) {
 			const int c = j / 192, f = (j / 32) % 6, k = j & 31, nb = s_nb[f];
 			uint32_t v = 0;
@@ -396,6 +399,11 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 					v = __ldg(level_plane(L, nb, c, t + 1) + k * 32); // z = 0, y = k
 			}
 			side[c][f][k] = v;
+		}
+#pragma unroll
+		for (int q = 0; q < kQ; ++q) {
+			const int j = tid + q * kLightThreads, c = j / (kPlaneWords / 4), o = j % (kPlaneWords / 4);
+			reinterpret_cast<uint4 *>(prev[c])[o] = own[q];
 		}
 	}
 	uint32_t pass[kLightRows], lows[kLightRows], s[kLightRows][2];
@@ -449,38 +457,41 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 			}
 		}
 	}
-	if (t == 1) {
-#pragma unroll 1
-		for (int k = 0; k < kLightRows; ++k) {
-			const int r = tid + k * kLightThreads;
-			uint32_t lv[kLevels], b[2][4];
+}
+
+// Light bytes of every cell of every batch chunk from its 15 level planes per channel (one thread
+// per row, a streaming pass).
+__global__ void __launch_bounds__(256) k_light_bytes(LightPass L) {
+	const uint64_t total = (uint64_t)L.n * kPlaneWords;
+	for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x) {
+		const int i = (int)(g >> 10), r = (int)(g & 1023u);
+		uint32_t b[2][4];
 #pragma unroll
-			for (int c = 0; c < 2; ++c) {
-				lv[0] = s[k][c];
+		for (int c = 0; c < 2; ++c) {
+			uint32_t lv[kLevels];
 #pragma unroll
-				for (int u = 2; u <= kLevels; ++u)
-					lv[u - 1] = __ldg(level_plane(L, i, c, u) + r);
-				level_bits(lv, b[c]);
-			}
-			uint32_t w[8];
-#pragma unroll
-			for (int q = 0; q < 8; ++q) {
-				uint32_t val = 0;
-#pragma unroll
-				for (int kk = 0; kk < 4; ++kk) {
-					const int x = 4 * q + kk;
-					uint32_t byte = 0;
-#pragma unroll
-					for (int bit = 0; bit < 4; ++bit)
-						byte |= ((b[0][bit] >> x) & 1u) << bit | ((b[1][bit] >> x) & 1u) << (bit + 4);
-					val |= byte << (8 * kk);
-				}
-				w[q] = val;
-			}
-			uint4 *dst = reinterpret_cast<uint4 *>(L.light + (size_t)i * 32768 + r * 32);
-			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
-			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+			for (int u = 1; u <= kLevels; ++u)
+				lv[u - 1] = __ldg(level_plane(L, i, c, u) + r);
+			level_bits(lv, b[c]);
 		}
+		uint32_t w[8];
+#pragma unroll
+		for (int q = 0; q < 8; ++q) {
+			uint32_t val = 0;
+#pragma unroll
+			for (int kk = 0; kk < 4; ++kk) {
+				const int x = 4 * q + kk;
+				uint32_t byte = 0;
+#pragma unroll
+				for (int bit = 0; bit < 4; ++bit)
+					byte |= ((b[0][bit] >> x) & 1u) << bit | ((b[1][bit] >> x) & 1u) << (bit + 4);
+				val |= byte << (8 * kk);
+			}
+			w[q] = val;
+		}
+		uint4 *dst = reinterpret_cast<uint4 *>(L.light + (size_t)i * 32768 + r * 32);
+		dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+		dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
 	}
 }
 
