@@ -221,6 +221,58 @@ __global__ void __launch_bounds__(kThreads, 1)
 	}
 }
 
+// Draw records of mesh descriptors (WorldRenderer::PushChunkMesh, WorldRenderer.hpp:69-87): the
+// float AABB is the u32 one in 1/16 voxel divided by 16, plus the chunk's base position.
+__global__ void k_mesh_infos(const hc_mesh_desc *meshes, uint32_t n, const int32_t *pos, hc_mesh_info *out) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	const hc_mesh_desc d = meshes[i];
+	hc_mesh_info m;
+	m.index_count = d.index_count;
+	m.first_index = d.index_offset;
+	m.vertex_offset = d.vertex_offset;
+	for (int c = 0; c < 3; ++c) {
+		const int32_t base = pos[3 * (size_t)d.chunk + c] * 32;
+		m.info.base_position[c] = base;
+		m.info.aabb_min[c] = __fadd_rn(__fdiv_rn((float)d.aabb_min[c], 16.0f), (float)base);
+		m.info.aabb_max[c] = __fadd_rn(__fdiv_rn((float)d.aabb_max[c], 16.0f), (float)base);
+	}
+	m.info.transparent = d.transparent;
+	out[i] = m;
+}
+
+// The same with the number of descriptors in device memory (an arena's mesh cursor, capped).
+__global__ void k_mesh_infos_dev(const hc_mesh_desc *meshes, const unsigned int *n_dev, uint32_t cap, const int32_t *pos,
+                                 hc_mesh_info *out) {
+	const uint32_t n = min(*n_dev, cap);
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const hc_mesh_desc d = meshes[i];
+		hc_mesh_info m;
+		m.index_count = d.index_count;
+		m.first_index = d.index_offset;
+		m.vertex_offset = d.vertex_offset;
+		for (int c = 0; c < 3; ++c) {
+			const int32_t base = pos[3 * (size_t)d.chunk + c] * 32;
+			m.info.base_position[c] = base;
+			m.info.aabb_min[c] = __fadd_rn(__fdiv_rn((float)d.aabb_min[c], 16.0f), (float)base);
+			m.info.aabb_max[c] = __fadd_rn(__fdiv_rn((float)d.aabb_max[c], 16.0f), (float)base);
+		}
+		m.info.transparent = d.transparent;
+		out[i] = m;
+	}
+}
+
+// Chunk positions of a world remesh list (for its draw records).
+__global__ void k_remesh_positions(WorldDev W, const int32_t *list, const uint32_t *n, int32_t *pos) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= *n)
+		return;
+	int ix, iy, iz;
+	cell_xyz(W, list[i], ix, iy, iz);
+	pos[3 * i] = W.cx0 + ix, pos[3 * i + 1] = W.cy0 + iy, pos[3 * i + 2] = W.cz0 + iz;
+}
+
 // Plain form at scale: one launch per chunk.
 __global__ void __launch_bounds__(kThreads, 1)
     k_mesh_item(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
@@ -651,6 +703,19 @@ hc_status hc_relight_chunk_device(hc_ctx *ctx, const uint16_t *const blocks[27],
 	return HC_OK;
 }
 
+hc_status hc_mesh_infos(hc_ctx *ctx, const hc_mesh_desc *meshes, uint32_t n, const int32_t *chunk_positions,
+                        hc_mesh_info *out, void *stream) {
+	if (!ctx || (n && (!meshes || !chunk_positions || !out)))
+		return HC_ERR_INVALID_ARG;
+	if (!n)
+		return HC_OK;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	k_mesh_infos<<<(n + 255) / 256, 256, 0, stream ? (cudaStream_t)stream : ctx->stream>>>(meshes, n, chunk_positions,
+	                                                                                        out);
+	HC_CUDA(ctx, cudaGetLastError());
+	return HC_OK;
+}
+
 hc_status hc_pool_create(hc_ctx *ctx, uint32_t capacity, hc_pool **out) {
 	if (!ctx || !out || capacity == 0)
 		return HC_ERR_INVALID_ARG;
@@ -1065,6 +1130,16 @@ hc_status world_enqueue_place(hc_world *w, const int32_t *d_pos, const int32_t *
 	return HC_OK;
 }
 
+hc_status world_enqueue_deltas(hc_world *w, const int32_t *d_slots, const uint32_t *d_boff, const uint32_t *d_soff,
+                               const uint32_t *d_blocks, const uint16_t *d_suns, uint32_t n, cudaStream_t st) {
+	if (n) {
+		const Deltas D{d_slots, d_boff, d_soff, d_blocks, d_suns, n};
+		k_apply_deltas<<<(n * 32 + 255) / 256, 256, 0, st>>>(D, w->pool->d_blocks, w->pool->d_heights);
+		HC_CUDA(w->ctx, cudaGetLastError());
+	}
+	return HC_OK;
+}
+
 hc_status world_enqueue_evict(hc_world *w, const int32_t *d_pos, uint32_t n, cudaStream_t st) {
 	if (n) {
 		k_evict<<<(n + 255) / 256, 256, 0, st>>>(d_pos, n, world_dev(w));
@@ -1130,6 +1205,16 @@ hc_status world_enqueue_remesh(hc_world *w, const hc_batch_arena *arena, cudaStr
 	return HC_OK;
 }
 
+hc_status world_enqueue_infos(hc_world *w, const hc_batch_arena *arena, int32_t *d_pos, hc_mesh_info *d_infos,
+                              cudaStream_t st) {
+	k_remesh_positions<<<(w->cells + 255) / 256, 256, 0, st>>>(world_dev(w), w->d_list, w->d_counts + kCountRemesh, d_pos);
+	HC_CUDA(w->ctx, cudaGetLastError());
+	k_mesh_infos_dev<<<std::max(1, std::min(w->sms * 4, (int)((arena->mesh_capacity + 255) / 256))), 256, 0, st>>>(
+	    arena->meshes, reinterpret_cast<const unsigned int *>(w->d_state + 1), arena->mesh_capacity, d_pos, d_infos);
+	HC_CUDA(w->ctx, cudaGetLastError());
+	return HC_OK;
+}
+
 Arena world_arena(const hc_world *w, const hc_batch_arena *arena) {
 	return Arena{reinterpret_cast<uint2 *>(arena->vertices),
 	             arena->indices,
@@ -1179,6 +1264,50 @@ hc_pool *world_pool(const hc_world *w) { return w->pool; }
 size_t pool_planes_bytes_per_slot() { return kPlaneStride * sizeof(uint32_t); }
 hc_status ctx_fail(hc_ctx *ctx, hc_status s, const std::string &msg) { return fail(ctx, s, msg); }
 int ctx_device(const hc_ctx *ctx) { return ctx->device; }
+
+// Stages the stored edits of a group of loads (one device buffer for the call) and applies them;
+// synchronous, as hc_world_load is.
+hc_status load_deltas(hc_world *w, const hc_chunk_load *loads, uint32_t n, cudaStream_t st) {
+	hc_ctx *ctx = w->ctx;
+	std::vector<int32_t> slots;
+	std::vector<uint32_t> boff(1, 0), soff(1, 0), blocks;
+	std::vector<uint16_t> suns;
+	for (uint32_t i = 0; i < n; ++i) {
+		const hc_chunk_load &l = loads[i];
+		if (!l.n_block_entries && !l.n_sunlight_entries)
+			continue;
+		slots.push_back(l.slot);
+		blocks.insert(blocks.end(), l.block_entries, l.block_entries + l.n_block_entries);
+		suns.insert(suns.end(), l.sunlight_entries, l.sunlight_entries + l.n_sunlight_entries);
+		boff.push_back((uint32_t)blocks.size());
+		soff.push_back((uint32_t)suns.size());
+	}
+	if (slots.empty())
+		return HC_OK;
+	const uint32_t m = (uint32_t)slots.size();
+	const size_t bytes = m * 4 + 2 * (m + 1) * 4 + blocks.size() * 4 + suns.size() * 2 + 16;
+	char *d = nullptr;
+	HC_CUDA(ctx, cudaMalloc(&d, bytes));
+	int32_t *d_slots = reinterpret_cast<int32_t *>(d);
+	uint32_t *d_boff = reinterpret_cast<uint32_t *>(d_slots + m), *d_soff = d_boff + m + 1, *d_blocks = d_soff + m + 1;
+	uint16_t *d_suns = reinterpret_cast<uint16_t *>(d_blocks + blocks.size());
+	cudaError_t e = cudaMemcpyAsync(d_slots, slots.data(), m * 4, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(d_boff, boff.data(), (m + 1) * 4, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(d_soff, soff.data(), (m + 1) * 4, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess && !blocks.empty())
+		e = cudaMemcpyAsync(d_blocks, blocks.data(), blocks.size() * 4, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess && !suns.empty())
+		e = cudaMemcpyAsync(d_suns, suns.data(), suns.size() * 2, cudaMemcpyHostToDevice, st);
+	hc_status s = e == cudaSuccess ? world_enqueue_deltas(w, d_slots, d_boff, d_soff, d_blocks, d_suns, m, st) : HC_OK;
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(st);
+	cudaFree(d);
+	if (e != cudaSuccess)
+		return fail(ctx, HC_ERR_CUDA, std::string("load: stored edits: ") + cudaGetErrorString(e));
+	return s;
+}
 
 } // namespace detail
 } // namespace hc
@@ -1295,6 +1424,10 @@ hc_status hc_world_load(hc_world *w, const hc_chunk_load *loads, uint32_t n, voi
 	for (uint32_t i = 0; i < n; ++i)
 		if (loads[i].slot < 0 || (uint32_t)loads[i].slot >= w->pool->capacity || !loads[i].blocks || !loads[i].heights)
 			return fail(ctx, HC_ERR_INVALID_ARG, "load: slot beyond the pool or data missing");
+	for (uint32_t i = 0; i < n; ++i)
+		if ((loads[i].n_block_entries && !loads[i].block_entries) ||
+		    (loads[i].n_sunlight_entries && !loads[i].sunlight_entries))
+			return fail(ctx, HC_ERR_INVALID_ARG, "load: stored edits missing");
 	cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
 	HC_CUDA(ctx, cudaSetDevice(ctx->device));
 	for (uint32_t first = 0; first < n; first += kStageChunks) {
@@ -1308,8 +1441,11 @@ hc_status hc_world_load(hc_world *w, const hc_chunk_load *loads, uint32_t n, voi
 			w->h_stage[3 * i] = l.cx, w->h_stage[3 * i + 1] = l.cy, w->h_stage[3 * i + 2] = l.cz;
 			w->h_stage[3 * nb + i] = l.slot;
 		}
+		hc_status s = load_deltas(w, loads + first, nb, st); // after the chunk data, before the placing
+		if (s != HC_OK)
+			return s;
 		HC_CUDA(ctx, cudaMemcpyAsync(w->d_stage, w->h_stage, 4 * nb * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-		const hc_status s = world_enqueue_place(w, w->d_stage, w->d_stage + 3 * nb, nb, st);
+		s = world_enqueue_place(w, w->d_stage, w->d_stage + 3 * nb, nb, st);
 		if (s != HC_OK)
 			return s;
 		HC_CUDA(ctx, cudaStreamSynchronize(st)); // the staging buffers are reused

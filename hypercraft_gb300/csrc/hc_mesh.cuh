@@ -34,6 +34,17 @@ struct Split {
 	__device__ __forceinline__ int owner(int p) const { return (p >> 1) % c; }
 };
 
+// Next index of a per-plane phase for the calling warp (all lanes get it): warps take planes as
+// they finish the previous one, so a phase ends when the work does, not when the unluckiest warp's
+// fixed share does.
+__device__ __forceinline__ int claim(uint32_t *counter) {
+	int j = 0;
+	if ((threadIdx.x & 31) == 0)
+		j = (int)atomicAdd(counter, 1u);
+	return __shfl_sync(0xffffffffu, j, 0);
+}
+enum : int { kClaimComplex = 12, kClaimKeys = 13, kClaimCount = 14 }; // S.misc counters
+
 struct Emit {
 	uint2 *verts;
 	uint16_t *idx;
@@ -104,8 +115,24 @@ __device__ __forceinline__ void put_quad(Smem &S, const Emit &E, int st, uint32_
 // when the chunk can produce no quad: every inner block has no texture and no custom mesh, or every
 // inner block and every block of the six adjacent layers is an opaque full cube.
 __device__ bool stage_classes(Smem &S, const DevTables &T) {
-	for (int i = threadIdx.x; i < 256; i += kThreads)
-		S.classes[i] = T.classes[i];
+	// With the planes, the chunk's own 32 KB of class ids are copied into the plane-mask scratch
+	// (unused until the light and plane passes) by asynchronous 16-byte copies, all in flight at
+	// once; the apron's class ids come straight from the neighbours' planes.
+	const uint8_t *own = reinterpret_cast<const uint8_t *>(&S.u);
+	if (S.pln[26]) {
+		const char *src = reinterpret_cast<const char *>(S.pln[26] + kPlaneClassOff);
+		const uint32_t dst = (uint32_t)__cvta_generic_to_shared(own);
+		for (int i = threadIdx.x; i < 32768 / 16; i += kThreads)
+			asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16 * i), "l"(src + 16 * i) : "memory");
+		asm volatile("cp.async.commit_group;" ::: "memory");
+	}
+	for (int i = threadIdx.x; i < 256; i += kThreads) {
+		const DevClass k = T.classes[i];
+		S.classes[i] = k;
+		S.cflags[i] = k.flags;
+	}
+	if (S.pln[26])
+		asm volatile("cp.async.wait_group 0;" ::: "memory");
 	__syncthreads();
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	constexpr int kRows = kCls * kCls, kBatch = 12; // 1156 rows; 12 in flight per warp
@@ -116,7 +143,8 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 #pragma unroll
 			for (int j = 0; j < kBatch; ++j) {
 				const int row = min(row0 + j, kRows - 1), y = row / kCls - 1, z = row % kCls - 1;
-				c[j] = class_byte(S, lane, y, z);
+				const bool inner = (unsigned)y < (unsigned)kChunk && (unsigned)z < (unsigned)kChunk;
+				c[j] = inner ? own[lane + (y * kChunk + z) * kChunk] : class_byte(S, lane, y, z);
 				ce[j] = lane < 2 ? class_byte(S, lane ? kChunk : -1, y, z) : (uint8_t)0;
 			}
 		} else {
@@ -142,7 +170,7 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 			dst[lane + 1] = (uint16_t)(c[j] << 8);
 			if (lane < 2)
 				dst[lane ? kCls - 1 : 0] = (uint16_t)(ce[j] << 8);
-			const uint8_t f = S.classes[c[j]].flags, fe = S.classes[ce[j]].flags;
+			const uint8_t f = S.cflags[c[j]], fe = S.cflags[ce[j]];
 			const uint32_t oc = __ballot_sync(0xffffffffu, f & kFOpaqueCube);
 			const uint32_t em = __ballot_sync(0xffffffffu, f & kFEmpty);
 			const uint32_t oce = __ballot_sync(0xffffffffu, lane < 2 && (fe & kFOpaqueCube));
@@ -337,8 +365,8 @@ __device__ void plane_visibility(Smem &S) {
 // Pass 1b: exact Show for the complex candidates of every plane row (texture lookups, dynamic
 // liquid textures), and transparent-pass bits of the faces it shows. Lane = plane row.
 __device__ void plane_complex(Smem &S, const Split &sp) {
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int j = warp; j < sp.planes(); j += kWarps) {
+	const int lane = threadIdx.x & 31;
+	for (int j = claim(&S.misc[kClaimComplex]); j < sp.planes(); j = claim(&S.misc[kClaimComplex])) {
 		const int p = sp.plane(j);
 		uint32_t *m = S.u.masks[p][lane];
 		uint32_t cx = m[1];
@@ -417,8 +445,8 @@ __device__ __forceinline__ Key face_key(const Smem &S, int a, int s, int inv, in
 // the light keys are computed by full warps; a face's right neighbour is the next lane and its
 // upper neighbour sits in this batch or in the previous one.
 __device__ void plane_keys(Smem &S, const Split &sp) {
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int j = warp; j < sp.planes(); j += kWarps) {
+	const int lane = threadIdx.x & 31;
+	for (int j = claim(&S.misc[kClaimKeys]); j < sp.planes(); j = claim(&S.misc[kClaimKeys])) {
 		const int p = sp.plane(j);
 		uint32_t *mrow = S.u.masks[p][lane];
 		const uint32_t N = mrow[0];
@@ -541,9 +569,9 @@ __device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, 
 // Counts the quads of every plane (warp per plane) and keeps their records in shared memory while
 // they fit; misc[4] = records kept, misc[5] = 1 if some did not fit.
 __device__ void planes_count(Smem &S, const Split &sp) {
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int lane = threadIdx.x & 31;
 	const uint32_t lt = (1u << lane) - 1u;
-	for (int j = warp; j < sp.planes(); j += kWarps) {
+	for (int j = claim(&S.misc[kClaimCount]); j < sp.planes(); j = claim(&S.misc[kClaimCount])) {
 		const int p = sp.plane(j);
 		uint32_t n_all = 0, n_st[2] = {0, 0};
 		warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
@@ -774,6 +802,8 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 	}
 	for (int i = tid; i < 2 * (kSegments + 1); i += kThreads)
 		S.seg_cnt[i / (kSegments + 1)][i % (kSegments + 1)] = 0;
+	if (tid < 3)
+		S.misc[kClaimComplex + tid] = 0; // the stage's barriers order this before the plane phases
 	const bool blank = stage_classes(S, T);
 
 	uint32_t qo = 0, qt = 0;

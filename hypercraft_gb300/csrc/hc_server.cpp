@@ -63,6 +63,7 @@ struct Admitted {
 };
 
 constexpr uint32_t kStatusOk = 0, kStatusRejected = 1;
+constexpr uint32_t kTickEntries = 1u << 20; // stored-edit entries per tick, of each kind
 constexpr uint64_t kStallNs = 20000000000ull; // 20 s without a completed request
 
 struct TickSlot {
@@ -77,6 +78,14 @@ struct TickSlot {
 	uint16_t *d_indices = nullptr;
 	hc_mesh_desc *d_meshes = nullptr;
 	uint32_t *d_results = nullptr;
+	int32_t *d_pos = nullptr;          // chunk positions of the remesh list
+	hc_mesh_info *d_infos = nullptr;   // the pass's draw records
+	// stored edits of the tick's loads: per load its slot and entry offsets, then the entries
+	int32_t *h_dslot = nullptr, *d_dslot = nullptr;
+	uint32_t *h_doff = nullptr, *d_doff = nullptr; // block offsets [L + 1], then sunlight offsets [L + 1]
+	uint32_t *h_bent = nullptr, *d_bent = nullptr;
+	uint16_t *h_sent = nullptr, *d_sent = nullptr;
+	uint32_t n_dchunks = 0, n_bent = 0, n_sent = 0;
 	cudaEvent_t start = nullptr, copied = nullptr, done = nullptr;
 	uint64_t index = 0;
 	std::vector<Admitted> reqs;
@@ -153,6 +162,9 @@ void admit(hc_server *s, TickSlot &t) {
 	int32_t *unload_pos = t.h_stage;
 	int32_t *load_pos = t.h_stage + 3 * c.max_loads_per_tick;
 	int32_t *load_slot = t.h_stage + 6 * c.max_loads_per_tick;
+	const uint32_t L = c.max_loads_per_tick;
+	t.n_dchunks = t.n_bent = t.n_sent = 0;
+	t.h_doff[0] = 0, t.h_doff[L + 1] = 0;
 	while (!s->queue.empty()) {
 		const Pending &p = s->queue.front();
 		const hc_request &r = p.req;
@@ -180,16 +192,34 @@ void admit(hc_server *s, TickSlot &t) {
 			}
 		} else if (r.kind == HC_REQ_LOAD || r.kind == HC_REQ_UNLOAD) {
 			const int cell = cell_of_chunk(s, r.x, r.y, r.z);
-			if (cell < 0 || (r.kind == HC_REQ_LOAD && (!r.blocks || !r.heights))) {
+			const bool bad_entries = r.kind == HC_REQ_LOAD &&
+			                         ((r.n_block_entries && !r.block_entries) ||
+			                          (r.n_sunlight_entries && !r.sunlight_entries) ||
+			                          r.n_block_entries > kTickEntries || r.n_sunlight_entries > kTickEntries);
+			if (cell < 0 || (r.kind == HC_REQ_LOAD && (!r.blocks || !r.heights)) || bad_entries) {
 				status = kStatusRejected;
 			} else {
 				if (edited.count(cell) || moved.count(cell) || nl + nu + 1 > c.max_loads_per_tick)
 					break;
+				if (r.kind == HC_REQ_LOAD && s->cell_slot[cell] < 0 &&
+				    (t.n_bent + r.n_block_entries > kTickEntries || t.n_sent + r.n_sunlight_entries > kTickEntries))
+					break; // the tick's room for stored edits is full
 				if (r.kind == HC_REQ_LOAD) {
 					if (s->cell_slot[cell] < 0) { // loading a resident chunk again changes nothing
 						if (s->free_slots.empty())
 							break; // waits for unloads to free a slot
 						const int32_t slot = s->free_slots.back();
+						if (r.n_block_entries || r.n_sunlight_entries) {
+							const uint32_t k = t.n_dchunks++;
+							t.h_dslot[k] = slot;
+							if (r.n_block_entries)
+								std::memcpy(t.h_bent + t.n_bent, r.block_entries, r.n_block_entries * 4);
+							if (r.n_sunlight_entries)
+								std::memcpy(t.h_sent + t.n_sent, r.sunlight_entries, r.n_sunlight_entries * 2);
+							t.n_bent += r.n_block_entries, t.n_sent += r.n_sunlight_entries;
+							t.h_doff[k + 1] = t.n_bent;
+							t.h_doff[L + 1 + k + 1] = t.n_sent;
+						}
 						s->free_slots.pop_back();
 						s->cell_slot[cell] = slot;
 						std::memcpy(t.h_blocks + (size_t)nl * 32768, r.blocks, 32768 * sizeof(uint16_t));
@@ -235,16 +265,27 @@ hc_status enqueue_pass(hc_server *s, TickSlot &t) {
 		SV_CUDA(s, cudaMemcpyAsync(pool_heights + (size_t)load_slot[i] * 1024, t.h_heights + (size_t)i * 1024, 1024,
 		                           cudaMemcpyHostToDevice, s->ks));
 	}
+	if (t.n_dchunks) {
+		SV_CUDA(s, cudaMemcpyAsync(t.d_dslot, t.h_dslot, t.n_dchunks * 4, cudaMemcpyHostToDevice, s->ks));
+		SV_CUDA(s, cudaMemcpyAsync(t.d_doff, t.h_doff, 2 * (L + 1) * 4, cudaMemcpyHostToDevice, s->ks));
+		if (t.n_bent)
+			SV_CUDA(s, cudaMemcpyAsync(t.d_bent, t.h_bent, t.n_bent * 4, cudaMemcpyHostToDevice, s->ks));
+		if (t.n_sent)
+			SV_CUDA(s, cudaMemcpyAsync(t.d_sent, t.h_sent, t.n_sent * 2, cudaMemcpyHostToDevice, s->ks));
+	}
 	SV_CUDA(s, cudaEventRecord(t.copied, s->ks));
 	SV_CUDA(s, cudaStreamWaitEvent(s->cs, t.copied, 0));
 	hc_status st;
-	if ((st = world_enqueue_evict(s->world, t.d_stage, t.n_unloads, s->cs)) != HC_OK ||
+	if ((st = world_enqueue_deltas(s->world, t.d_dslot, t.d_doff, t.d_doff + L + 1, t.d_bent, t.d_sent, t.n_dchunks,
+	                               s->cs)) != HC_OK ||
+	    (st = world_enqueue_evict(s->world, t.d_stage, t.n_unloads, s->cs)) != HC_OK ||
 	    (st = world_enqueue_place(s->world, t.d_stage + 3 * L, t.d_stage + 6 * L, t.n_loads, s->cs)) != HC_OK ||
 	    (st = world_enqueue_edits(s->world, t.d_edits, t.n_edits, s->cs)) != HC_OK ||
 	    (t.n_edits && (st = world_enqueue_heights(s->world, s->cs)) != HC_OK))
 		return st;
 	hc_batch_arena a{c.arena_quads, c.arena_meshes, t.d_vertices, t.d_indices, t.d_meshes, t.d_results};
-	if ((st = world_enqueue_remesh(s->world, &a, s->cs)) != HC_OK)
+	if ((st = world_enqueue_remesh(s->world, &a, s->cs)) != HC_OK ||
+	    (st = world_enqueue_infos(s->world, &a, t.d_pos, t.d_infos, s->cs)) != HC_OK)
 		return st;
 	SV_CUDA(s, cudaMemcpyAsync(t.h_counts, world_counts(s->world), kWorldCountWords * sizeof(uint32_t),
 	                           cudaMemcpyDeviceToHost, s->cs));
@@ -324,16 +365,20 @@ bool finish_tick(hc_server *s, bool block) {
 		std::vector<uint32_t> res((size_t)n * 5), verts((size_t)quads * 8);
 		std::vector<uint16_t> idx((size_t)quads * 6);
 		std::vector<hc_mesh_desc> md(meshes);
+		std::vector<hc_mesh_info> mi(meshes);
 		if (n)
 			cudaMemcpyAsync(res.data(), t.d_results, res.size() * 4, cudaMemcpyDeviceToHost, s->ss);
 		if (quads) {
 			cudaMemcpyAsync(verts.data(), t.d_vertices, verts.size() * 4, cudaMemcpyDeviceToHost, s->ss);
 			cudaMemcpyAsync(idx.data(), t.d_indices, idx.size() * 2, cudaMemcpyDeviceToHost, s->ss);
 		}
-		if (meshes)
+		if (meshes) {
 			cudaMemcpyAsync(md.data(), t.d_meshes, md.size() * sizeof(hc_mesh_desc), cudaMemcpyDeviceToHost, s->ss);
+			cudaMemcpyAsync(mi.data(), t.d_infos, mi.size() * sizeof(hc_mesh_info), cudaMemcpyDeviceToHost, s->ss);
+		}
 		cudaStreamSynchronize(s->ss);
-		s->sink(s->sink_user, t.index, n, t.h_cells, res.data(), verts.data(), idx.data(), md.data(), quads, meshes);
+		s->sink(s->sink_user, t.index, n, t.h_cells, res.data(), verts.data(), idx.data(), md.data(), mi.data(), quads,
+		        meshes);
 	}
 	std::lock_guard<std::mutex> lk(s->mu);
 	for (const Admitted &a : t.reqs) {
@@ -394,8 +439,11 @@ void free_slot(TickSlot &t) {
 	cudaFreeHost(t.h_counts);
 	cudaFreeHost(t.h_state);
 	cudaFreeHost(t.h_cells);
+	for (void *p : {(void *)t.h_dslot, (void *)t.h_doff, (void *)t.h_bent, (void *)t.h_sent})
+		cudaFreeHost(p);
 	for (void *p : {(void *)t.d_edits, (void *)t.d_stage, (void *)t.d_vertices, (void *)t.d_indices, (void *)t.d_meshes,
-	                (void *)t.d_results})
+	                (void *)t.d_results, (void *)t.d_dslot, (void *)t.d_doff, (void *)t.d_bent, (void *)t.d_sent,
+	                (void *)t.d_pos, (void *)t.d_infos})
 		cudaFree(p);
 	for (cudaEvent_t e : {t.start, t.copied, t.done})
 		if (e)
@@ -445,6 +493,16 @@ hc_status hc_server_create(hc_ctx *ctx, const hc_world_desc *desc, uint32_t pool
 		A((void **)&t.d_indices, config->arena_quads * 6 * sizeof(uint16_t) + 4);
 		A((void **)&t.d_meshes, (size_t)config->arena_meshes * sizeof(hc_mesh_desc));
 		A((void **)&t.d_results, (size_t)cells * 5 * sizeof(uint32_t));
+		A((void **)&t.d_pos, (size_t)cells * 3 * sizeof(int32_t));
+		A((void **)&t.d_infos, (size_t)config->arena_meshes * sizeof(hc_mesh_info));
+		H((void **)&t.h_dslot, L * sizeof(int32_t));
+		A((void **)&t.d_dslot, L * sizeof(int32_t));
+		H((void **)&t.h_doff, 2 * (L + 1) * sizeof(uint32_t));
+		A((void **)&t.d_doff, 2 * (L + 1) * sizeof(uint32_t));
+		H((void **)&t.h_bent, kTickEntries * sizeof(uint32_t));
+		A((void **)&t.d_bent, kTickEntries * sizeof(uint32_t));
+		H((void **)&t.h_sent, kTickEntries * sizeof(uint16_t));
+		A((void **)&t.d_sent, kTickEntries * sizeof(uint16_t));
 		if (e == cudaSuccess)
 			e = cudaEventCreate(&t.start);
 		if (e == cudaSuccess)

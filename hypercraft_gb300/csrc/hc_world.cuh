@@ -246,6 +246,46 @@ __global__ void k_place(const int32_t *pos, const int32_t *slot, uint32_t n, Wor
 	}
 }
 
+// Stored edits of loaded chunks (common/include/common/Data.hpp:36-86): chunk k of the batch lives
+// in slot[k]; its block entries are blocks[boff[k], boff[k + 1]) and its sunlight entries
+// suns[soff[k], soff[k + 1]).
+struct Deltas {
+	const int32_t *slot;
+	const uint32_t *boff, *soff;
+	const uint32_t *blocks; // cell index << 16 | raw block
+	const uint16_t *suns;   // column index << 6 | height
+	uint32_t n;
+};
+
+// One warp per loaded chunk applies its entries in order, as ChunkTaskRunner<kGenerate>::Run
+// calls SetBlock / SetSunlightHeight for each (client/src/ChunkGenerateTask.cpp:33-36): within
+// each group of 32 the last entry of a cell wins, and groups go in order.
+__global__ void k_apply_deltas(Deltas D, uint16_t *pool_blocks, int8_t *pool_heights) {
+	const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (w >= D.n)
+		return;
+	const size_t slot = (size_t)D.slot[w];
+	for (uint32_t i0 = D.boff[w]; i0 < D.boff[w + 1]; i0 += 32) {
+		const uint32_t i = i0 + lane;
+		const bool valid = i < D.boff[w + 1] && (D.blocks[i] >> 16) < 32768u;
+		const uint32_t e = valid ? D.blocks[i] : 0u;
+		const uint32_t peers = __match_any_sync(0xffffffffu, valid ? (e >> 16) : 0x10000u + lane);
+		if (valid && lane == 31 - __clz(peers))
+			pool_blocks[slot * 32768 + (e >> 16)] = (uint16_t)(e & 0xffffu);
+		__syncwarp();
+	}
+	for (uint32_t i0 = D.soff[w]; i0 < D.soff[w + 1]; i0 += 32) {
+		const uint32_t i = i0 + lane;
+		const bool valid = i < D.soff[w + 1];
+		const uint32_t e = valid ? D.suns[i] : 0u;
+		const uint32_t peers = __match_any_sync(0xffffffffu, valid ? (e >> 6) : 0x10000u + lane);
+		if (valid && lane == 31 - __clz(peers))
+			pool_heights[slot * 1024 + (e >> 6)] = (int8_t)(e & 63u);
+		__syncwarp();
+	}
+}
+
 // Takes n chunks out of the grid (ChunkTaskData<kMesh>::OnUnload drops a queued remesh too).
 __global__ void k_evict(const int32_t *pos, uint32_t n, WorldDev W) {
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;

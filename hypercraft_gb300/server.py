@@ -23,9 +23,11 @@ from .mesher import BlockMesh, Context, HcError, MESH_DESC_DTYPE, library
 
 REQ_EDIT, REQ_FILL, REQ_LOAD, REQ_UNLOAD = 0, 1, 2, 3
 
-REQUEST_DTYPE = np.dtype({"names": ["kind", "block", "x", "y", "z", "size", "blocks", "heights", "tag"],
-                          "formats": ["<u4", "<u4", "<i4", "<i4", "<i4", "<u4", "<u8", "<u8", "<u8"],
-                          "offsets": [0, 4, 8, 12, 16, 20, 24, 32, 40], "itemsize": 48})
+REQUEST_DTYPE = np.dtype({"names": ["kind", "block", "x", "y", "z", "size", "blocks", "heights", "tag", "block_entries",
+                                    "sunlight_entries", "n_block_entries", "n_sunlight_entries"],
+                          "formats": ["<u4", "<u4", "<i4", "<i4", "<i4", "<u4", "<u8", "<u8", "<u8", "<u8", "<u8", "<u4",
+                                      "<u4"],
+                          "offsets": [0, 4, 8, 12, 16, 20, 24, 32, 40, 48, 56, 64, 68], "itemsize": 72})
 COMPLETION_DTYPE = np.dtype({"names": ["tag", "kind", "status", "tick", "submit_ns", "done_ns"],
                              "formats": ["<u8", "<u4", "<u4", "<u8", "<u8", "<u8"],
                              "offsets": [0, 8, 12, 16, 24, 32], "itemsize": 40})
@@ -52,7 +54,27 @@ class ServerStats(ctypes.Structure):
 
 
 SINK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
-                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32)
+                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                        ctypes.c_uint32)
+
+# MeshInfo<ChunkMeshInfo> (client/include/client/mesh/MeshInfo.hpp:9-12, ChunkMesh.hpp:12-18)
+MESH_INFO_DTYPE = np.dtype([("index_count", "<u4"), ("first_index", "<u4"), ("vertex_offset", "<u4"),
+                            ("aabb_min", "<f4", 3), ("aabb_max", "<f4", 3), ("base_position", "<i4", 3),
+                            ("transparent", "<u4")])
+
+
+def mesh_info_of(desc, chunk_pos) -> np.void:
+    """Host restatement of WorldRenderer::PushChunkMesh's record (WorldRenderer.hpp:69-87):
+    (fAABB)aabb / 16 + base, in float32."""
+    out = np.zeros(1, MESH_INFO_DTYPE)[0]
+    base = np.asarray(chunk_pos, np.int32) * 32
+    out["index_count"], out["first_index"], out["vertex_offset"] = desc["index_count"], desc["index_offset"], \
+        desc["vertex_offset"]
+    out["aabb_min"] = np.asarray(desc["aabb_min"], np.uint32).astype(np.float32) / np.float32(16) + base.astype(np.float32)
+    out["aabb_max"] = np.asarray(desc["aabb_max"], np.uint32).astype(np.float32) / np.float32(16) + base.astype(np.float32)
+    out["base_position"] = base
+    out["transparent"] = desc["transparent"]
+    return out
 
 
 def _bind(lib):
@@ -170,7 +192,7 @@ class Server:
             self.ctx.check(self.lib.hc_server_set_sink(self.handle, SINK(), None), "hc_server_set_sink")
             return
 
-        def cb(_user, tick, n, cells_p, results_p, verts_p, idx_p, meshes_p, quads, mesh_count):
+        def cb(_user, tick, n, cells_p, results_p, verts_p, idx_p, meshes_p, infos_p, quads, mesh_count):
             cells = np.ctypeslib.as_array(ctypes.cast(cells_p, ctypes.POINTER(ctypes.c_int32)), (n,)).copy() if n else \
                 np.empty(0, np.int32)
             res = np.ctypeslib.as_array(ctypes.cast(results_p, ctypes.POINTER(ctypes.c_uint32)), (n * 5,)).reshape(-1, 5) \
@@ -181,6 +203,8 @@ class Server:
                 else np.empty(0, np.uint16)
             md = np.frombuffer(ctypes.string_at(meshes_p, mesh_count * MESH_DESC_DTYPE.itemsize), MESH_DESC_DTYPE) \
                 if mesh_count else np.empty(0, MESH_DESC_DTYPE)
+            mi = np.frombuffer(ctypes.string_at(infos_p, mesh_count * MESH_INFO_DTYPE.itemsize), MESH_INFO_DTYPE) \
+                if mesh_count else np.empty(0, MESH_INFO_DTYPE)
             per_chunk = []
             for i in range(n):
                 r = res[i]
@@ -194,7 +218,10 @@ class Server:
                                         tuple(int(x) for x in d["aabb_min"]) + tuple(int(x) for x in d["aabb_max"]),
                                         bool(d["transparent"])))
                 per_chunk.append(ms)
-            fn(int(tick), cells, per_chunk, res[:, 4].copy())
+            if getattr(fn, "wants_infos", False):
+                fn(int(tick), cells, per_chunk, res[:, 4].copy(), md.copy(), mi.copy())
+            else:
+                fn(int(tick), cells, per_chunk, res[:, 4].copy())
 
         self._sink = SINK(cb)
         self.ctx.check(self.lib.hc_server_set_sink(self.handle, self._sink, None), "hc_server_set_sink")

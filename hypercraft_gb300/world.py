@@ -22,7 +22,32 @@ class _Desc(ctypes.Structure):
 
 class ChunkLoad(ctypes.Structure):
     _fields_ = [("cx", ctypes.c_int32), ("cy", ctypes.c_int32), ("cz", ctypes.c_int32), ("slot", ctypes.c_int32),
-                ("blocks", ctypes.c_void_p), ("heights", ctypes.c_void_p)]
+                ("blocks", ctypes.c_void_p), ("heights", ctypes.c_void_p), ("block_entries", ctypes.c_void_p),
+                ("sunlight_entries", ctypes.c_void_p), ("n_block_entries", ctypes.c_uint32),
+                ("n_sunlight_entries", ctypes.c_uint32)]
+
+
+def pack_block_entries(cells, blocks) -> np.ndarray:
+    """PackedChunkBlockEntry (common/include/common/Data.hpp:36-58): cell index << 16 | raw block."""
+    return (np.asarray(cells, np.uint32) << 16) | (np.asarray(blocks, np.uint32) & 0xFFFF)
+
+
+def pack_sunlight_entries(columns, heights) -> np.ndarray:
+    """PackedChunkSunlightEntry (common/include/common/Data.hpp:60-81): column index << 6 | height."""
+    return ((np.asarray(columns, np.uint32) << 6) | (np.asarray(heights, np.uint32) & 63)).astype(np.uint16)
+
+
+def apply_entries(blocks, heights, block_entries=None, sunlight_entries=None):
+    """Host restatement of loading a chunk's stored edits (ChunkGenerateTask.cpp:33-36), in order."""
+    blocks, heights = blocks.copy(), heights.copy()
+    for e in (block_entries if block_entries is not None else []):
+        e = int(e)
+        if (e >> 16) < 32768:
+            blocks[e >> 16] = e & 0xFFFF
+    for e in (sunlight_entries if sunlight_entries is not None else []):
+        e = int(e)
+        heights[e >> 6] = np.int8(e & 63)
+    return blocks, heights
 
 
 def _bind(lib):
@@ -72,17 +97,25 @@ class ResidentWorld:
             self.ctx.check(self.lib.hc_world_apply_edits(self.handle, e.ctypes.data, len(e), 0, stream),
                            "hc_world_apply_edits")
 
-    def load(self, cells, blocks=None, heights=None, stream=None):
+    def load(self, cells, blocks=None, heights=None, stream=None, entries=None):
         """Loads grid cells (chunk i into pool slot i) from the world's arrays, or from the given
-        (n, 32768) blocks and (n, 1024) heights."""
+        (n, 32768) blocks and (n, 1024) heights; entries: optional per-chunk (block_entries,
+        sunlight_entries) of stored edits, applied on the device after the copy."""
         cells = np.asarray(cells, np.int64)
         b = np.ascontiguousarray(self.world.blocks[cells] if blocks is None else blocks, np.uint16)
         h = np.ascontiguousarray(self.world.heights[cells] if heights is None else heights, np.int8)
         loads = (ChunkLoad * len(cells))()
+        keep = []
         for i, c in enumerate(cells):
             ix, iy, iz = self.world.coords(int(c))
             ox, oy, oz = self.world.origin
-            loads[i] = ChunkLoad(ox + ix, oy + iy, oz + iz, int(c), b[i].ctypes.data, h[i].ctypes.data)
+            be, se = (entries[i] if entries is not None else (None, None))
+            be = np.ascontiguousarray(be if be is not None else np.zeros(0), np.uint32)
+            se = np.ascontiguousarray(se if se is not None else np.zeros(0), np.uint16)
+            keep += [be, se]
+            loads[i] = ChunkLoad(ox + ix, oy + iy, oz + iz, int(c), b[i].ctypes.data, h[i].ctypes.data,
+                                 be.ctypes.data if len(be) else None, se.ctypes.data if len(se) else None,
+                                 len(be), len(se))
         self.ctx.check(self.lib.hc_world_load(self.handle, loads, len(cells), stream), "hc_world_load")
 
     def unload(self, cells, stream=None):

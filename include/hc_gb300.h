@@ -139,6 +139,26 @@ typedef struct hc_batch_arena {
 	uint32_t *results;
 } hc_batch_arena;
 
+/* The renderer's hand-off records (client/include/client/ChunkMesh.hpp:12-18 and
+ * client/include/client/mesh/MeshInfo.hpp:9-12): ChunkMeshInfo (40 bytes) and the
+ * MeshInfo<ChunkMeshInfo> draw record (52 bytes) that WorldRenderer::PushChunkMesh builds for each
+ * mesh (client/include/client/WorldRenderer.hpp:69-87): the AABB in world units as float, the
+ * u32 AABB (1/16 voxel) divided by 16 plus the chunk's base position. */
+typedef struct hc_chunk_mesh_info {
+	float aabb_min[3], aabb_max[3];
+	int32_t base_position[3]; /* chunk position * 32 */
+	uint32_t transparent;
+} hc_chunk_mesh_info;
+typedef struct hc_mesh_info {
+	uint32_t index_count, first_index, vertex_offset; /* into the arena's index and vertex buffers */
+	hc_chunk_mesh_info info;
+} hc_mesh_info;
+
+/* Draw records for `n` mesh descriptors of an arena (device arrays): chunk i of the batch (the
+ * descriptor's `chunk`) is at chunk_positions[3i .. 3i+2] (device int32). Asynchronous. */
+hc_status hc_mesh_infos(hc_ctx *ctx, const hc_mesh_desc *meshes, uint32_t n, const int32_t *chunk_positions,
+                        hc_mesh_info *out, void *stream);
+
 typedef struct hc_batch_plan hc_batch_plan;
 
 enum { HC_BATCH_PERSISTENT = 0, HC_BATCH_PER_CHUNK = 1 };
@@ -200,13 +220,20 @@ void hc_world_destroy(hc_world *world);
 hc_status hc_world_apply_edits(hc_world *world, const hc_edit *edits, uint32_t n, int src_on_device, void *stream);
 
 /* A chunk entering the world (replaces ChunkTaskRunner<kGenerate>::Run,
- * client/src/ChunkGenerateTask.cpp:22-42): its blocks (32768 uint16) and sunlight heights
- * (1024 int8), host memory, are copied into pool slot `slot`, and it is marked for remeshing. */
+ * client/src/ChunkGenerateTask.cpp:22-42): its generated blocks (32768 uint16) and sunlight
+ * heights (1024 int8), host memory, are copied into pool slot `slot`; then its stored edits are
+ * applied in order, as the reference applies a ChunkEntry from its database: block entries in the
+ * PackedChunkBlockEntry layout (uint32: cell index << 16 | raw block) and sunlight entries in the
+ * PackedChunkSunlightEntry layout (uint16: column index << 6 | height)
+ * (common/include/common/Data.hpp:36-86). The chunk is then marked for remeshing. */
 typedef struct hc_chunk_load {
 	int32_t cx, cy, cz; /* chunk position */
 	int32_t slot;       /* free pool slot */
 	const uint16_t *blocks;
 	const int8_t *heights;
+	const uint32_t *block_entries;   /* may be NULL when n_block_entries is 0 */
+	const uint16_t *sunlight_entries;
+	uint32_t n_block_entries, n_sunlight_entries;
 } hc_chunk_load;
 
 /* Loads `n` chunks (positions outside the grid are skipped). Each is marked for remeshing, and so
@@ -267,6 +294,9 @@ typedef struct hc_request {
 	const uint16_t *blocks; /* LOAD: 32768 blocks (host), read when the request is admitted */
 	const int8_t *heights;  /* LOAD: 1024 sunlight heights (host) */
 	uint64_t tag;           /* echoed in the completion */
+	const uint32_t *block_entries;    /* LOAD: stored edits, as in hc_chunk_load (host) */
+	const uint16_t *sunlight_entries;
+	uint32_t n_block_entries, n_sunlight_entries;
 } hc_request;
 
 typedef struct hc_completion {
@@ -286,11 +316,13 @@ typedef struct hc_server_stats {
 } hc_server_stats;
 
 /* Called on the server's completion thread after each pass, with host copies of its output: the
- * remeshed grid cells, their result words (5 each), and the arena's vertices, indices and mesh
- * descriptors (offsets as in hc_batch_arena). For tests and tools: it costs a full read-back. */
+ * remeshed grid cells, their result words (5 each), and the arena's vertices, indices, mesh
+ * descriptors (offsets as in hc_batch_arena) and draw records. Every pass computes the draw
+ * records on the device; the sink, for tests and tools, costs a full read-back. */
 typedef void (*hc_tick_sink)(void *user, uint64_t tick, uint32_t n_chunks, const int32_t *cells,
                              const uint32_t *results, const uint32_t *vertices, const uint16_t *indices,
-                             const hc_mesh_desc *meshes, uint64_t quads, uint32_t mesh_count);
+                             const hc_mesh_desc *meshes, const hc_mesh_info *infos, uint64_t quads,
+                             uint32_t mesh_count);
 
 /* Creates a server over an empty world grid with a chunk pool of `pool_capacity` slots (0: as many
  * as free device memory allows, keeping 2 GiB, at most 65536). */

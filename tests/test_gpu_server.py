@@ -162,3 +162,56 @@ def test_rejects_and_slot_reuse(ctx, library):
     assert res[srv.cell(-4, 0, 0)] == -1 and res[srv.cell(0, 1, 0)] >= 0
     assert srv.stats()["resident"] == 8
     srv.close()
+
+
+def test_loads_with_stored_edits(ctx, library):
+    """A LOAD request's stored edits are applied after its data, before it is meshed."""
+    from hypercraft_gb300 import server as hs, world as hw
+    srv = hs.Server(ctx, GRID, ORIGIN, pool_capacity=64, max_loads_per_tick=8, arena_quads=1 << 20,
+                    arena_meshes=4096)
+    rng = np.random.default_rng(5)
+    k = library.index(0, 0, 0)
+    be = hw.pack_block_entries(rng.integers(0, 32768, 500), rng.choice([0, 1, 24], 500))
+    se = hw.pack_sunlight_entries(rng.integers(0, 1024, 50), rng.integers(0, 33, 50))
+    r = np.zeros(2, hs.REQUEST_DTYPE)
+    for i, (x, with_entries) in enumerate(((0, True), (1, False))):
+        r[i]["kind"], r[i]["x"], r[i]["y"], r[i]["z"] = hs.REQ_LOAD, x, 0, 0
+        r[i]["blocks"], r[i]["heights"] = library.blocks[k].ctypes.data, library.heights[k].ctypes.data
+        if with_entries:
+            r[i]["block_entries"], r[i]["n_block_entries"] = be.ctypes.data, len(be)
+            r[i]["sunlight_entries"], r[i]["n_sunlight_entries"] = se.ctypes.data, len(se)
+    srv.submit(r)
+    srv.drain()
+    b, h = srv.download([srv.cell(0, 0, 0), srv.cell(1, 0, 0)])
+    wb, wh = hw.apply_entries(library.blocks[k], library.heights[k], be, se)
+    assert np.array_equal(b[0], wb) and np.array_equal(h[0], wh)
+    assert np.array_equal(b[1], library.blocks[k]) and np.array_equal(h[1], library.heights[k])
+    srv.close()
+
+
+def test_draw_records_match_the_renderer_rule(ctx, library):
+    """Every pass's MeshInfo<ChunkMeshInfo> records equal WorldRenderer::PushChunkMesh's: the arena
+    offsets and counts, and the float AABB = u32 AABB / 16 + chunk base (bit for bit)."""
+    from hypercraft_gb300 import server as hs
+    srv = _server(ctx)
+    init, _, _ = _trace(library)
+    errors, seen = [], [0]
+
+    def sink(tick, cells, meshes, status, md, mi):
+        try:
+            for j in range(len(md)):
+                c = int(cells[int(md[j]["chunk"])])
+                want = hs.mesh_info_of(md[j], srv.cell_pos(c))
+                if want.tobytes() != mi[j].tobytes():
+                    errors.append((tick, j, want, mi[j]))
+                seen[0] += 1
+        except Exception as e:  # noqa: BLE001
+            errors.append(repr(e))
+
+    sink.wants_infos = True
+    srv.set_sink(sink)
+    srv.submit(init)
+    srv.drain()
+    assert not errors, errors[:3]
+    assert seen[0] > 50
+    srv.close()

@@ -155,3 +155,41 @@ def test_full_arena_requeues_only_what_did_not_fit(ctx, oracle):
         got = big.chunk_meshes(i, host)
         assert len(got) == len(want) and all(x == y for x, y in zip(got, want)), int(c)
     assert len(rw.remesh(big)[0]) == 0
+
+
+def test_loads_apply_stored_edits(ctx, oracle):
+    """A loaded chunk's stored edits (the reference's packed block and sunlight entries) are applied
+    in order after its generated data, and the chunk is meshed from the result."""
+    from hypercraft_gb300 import batch, world as hw
+    w = hw.edit_world()
+    rng = np.random.default_rng(21)
+    cells = [w.index(3, 2, 3), w.index(4, 2, 3)]
+    resident = np.ones(w.n_chunks, bool)
+    resident[cells] = False
+    rw = hw.ResidentWorld(ctx, w, resident=resident)
+    entries, want_b, want_h = [], [], []
+    for c in cells:
+        idx = rng.integers(0, 32768, 3000)
+        idx[-100:] = idx[:100]  # the same cell edited twice: the later entry wins
+        blk = rng.choice([0, 1, 9, 14, 16, 24], size=len(idx))
+        cols = rng.integers(0, 1024, 200)
+        hts = rng.integers(0, 33, 200)
+        be, se = hw.pack_block_entries(idx, blk), hw.pack_sunlight_entries(cols, hts)
+        entries.append((be, se))
+        b, h = hw.apply_entries(w.blocks[c], w.heights[c], be, se)
+        want_b.append(b)
+        want_h.append(h)
+    rw.load(cells, entries=entries)
+    got_b, got_h = rw.download()
+    for k, c in enumerate(cells):
+        assert np.array_equal(got_b[c], want_b[k]) and np.array_equal(got_h[c], want_h[k])
+    arena = batch.Arena(4_000_000, 8192, w.n_chunks)
+    remeshed, _, _ = rw.remesh(arena)
+    assert sorted(int(c) for c in remeshed) == sorted(cells)
+    w.blocks[cells] = np.stack(want_b)
+    w.heights[cells] = np.stack(want_h)
+    host = arena.host()
+    for i, c in enumerate(remeshed):
+        want = _meshes_of_chunk(oracle, w, c)
+        got = arena.chunk_meshes(i, host)
+        assert len(got) == len(want) and all(x == y for x, y in zip(got, want)), int(c)

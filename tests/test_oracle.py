@@ -113,3 +113,15 @@ def test_seeded_edits_are_deterministic():
     assert np.array_equal(a, b)
     d = np.sqrt((a["x"] - 16.0) ** 2 + (a["y"] - 16.0) ** 2 + (a["z"] - 16.0) ** 2)
     assert d.max() <= 48 and 0.05 < np.mean(a["block"] == 24) < 0.15
+
+
+def test_stored_edit_entries_pack_like_the_reference():
+    """PackedChunkBlockEntry / PackedChunkSunlightEntry bit layouts (common/include/common/Data.hpp:36-86)."""
+    from hypercraft_gb300 import world as hw
+    be = hw.pack_block_entries([0, 32767, 1234], [0x0201, 0xffff, 9])
+    assert list(be) == [0x0201, (32767 << 16) | 0xffff, (1234 << 16) | 9]
+    se = hw.pack_sunlight_entries([0, 1023, 77], [0, 32, 5])
+    assert se.dtype == np.uint16 and list(se) == [0, (1023 << 6) | 32, (77 << 6) | 5]
+    b, h = hw.apply_entries(np.zeros(32768, np.uint16), np.zeros(1024, np.int8),
+                            hw.pack_block_entries([5, 5], [1, 2]), hw.pack_sunlight_entries([3], [17]))
+    assert b[5] == 2 and h[3] == 17
