@@ -475,16 +475,18 @@ __device__ void plane_keys(Smem &S, const Split &sp) {
 			const int ue = over ? __ffs(over) - 1 : 32;
 			const uint32_t be = __shfl_sync(0xffffffffu, start, ue & 31);
 			const uint32_t bend = ue < 32 ? be : total;
-			// this lane's face: compacted index f = b + lane
+			// this lane's face: compacted index f = b + lane. The batch starts at row ub's first face
+			// and every row holds at most 32 faces, so the rows of the batch that hold faces start
+			// at distinct lanes: lane j's row is the m-th of them, m = the row starts at or below j.
 			const uint32_t f = b + lane;
 			const bool has = f < bend;
-			int u = 0;
-			uint32_t k = 0;
-			for (int r = ub; r < ue; ++r) {
-				const uint32_t rs = __shfl_sync(0xffffffffu, start, r), rc = __shfl_sync(0xffffffffu, cnt, r);
-				if (f >= rs && f < rs + rc)
-					u = r, k = f - rs;
-			}
+			const bool rin = lane >= ub && lane < ue && cnt > 0;
+			const uint32_t R = __ballot_sync(0xffffffffu, rin);
+			const uint32_t M = __reduce_or_sync(0xffffffffu, rin ? 1u << (start - b) : 0u);
+			const uint32_t upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+			const int u = has ? nth_set_bit(R, (uint32_t)__popc(M & upto) - 1u) : 0;
+			const uint32_t su = __shfl_sync(0xffffffffu, start, u); // every lane takes part
+			const uint32_t k = has ? f - su : 0u;
 			const uint32_t Nu = __shfl_sync(0xffffffffu, N, u);
 			const int v = has ? nth_set_bit(Nu, k) : 0;
 			Key key{0, 0, 0};
