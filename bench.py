@@ -373,8 +373,8 @@ def ours(args):
                          "peak_source": f"{peak_kind} ({'MEASURED_PEAKS.json hbm_gbs' if peak_kind == 'measured' else 'fallback'})",
                          "algorithmic_bytes_per_launch": algo_bytes},
             "serving": serving,
-            # per step the plan's graph runs 18 kernels: planes, 15 light levels, light bytes, mesh
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * 18,
+            # per step the plan's graph runs 17 kernels: planes, 15 light levels, mesh
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * 17,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

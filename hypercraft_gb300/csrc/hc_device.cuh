@@ -114,7 +114,8 @@ struct Smem {
 	const uint16_t *blk[27];
 	const int8_t *hgt[27];
 	const uint32_t *pln[27]; // per-chunk bit planes, or null (then the window is seeded from blocks)
-	const uint8_t *lgt[27];  // per-chunk light from the batch light pass, or null (then relight the window)
+	const uint32_t *lvl[27]; // per-chunk level planes of the batch light pass, or null (then relight the window)
+	const uint32_t *edg[27]; // ... and their x = 0 / x = 31 edge bits
 	alignas(16) uint16_t cell[kClsCells + 8]; // per cell of [-1, 32]^3: light (low byte), class id (high byte)
 	union {
 		Relight rl;
@@ -133,6 +134,8 @@ struct Smem {
 	uint32_t aabb[2][kMaxMeshesPerStream][6];
 	uint32_t trig[2][kMaxMeshesPerStream];
 	uint32_t misc[16];
+	uint8_t plane_owner[kPlanes]; // cluster form, in CTA 0: the CTA that took each face plane
+	uint8_t mine[kPlanes];        // the face planes this CTA took, in the order it took them
 };
 
 __device__ __forceinline__ int cls_index(int x, int y, int z) { return ((y + 1) * kCls + (z + 1)) * kCls + (x + 1); }

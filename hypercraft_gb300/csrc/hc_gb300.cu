@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mesh_single(Refs27 refs, DevTab
 		S.blk[threadIdx.x] = refs.blk[threadIdx.x];
 		S.hgt[threadIdx.x] = refs.hgt[threadIdx.x];
 		S.pln[threadIdx.x] = refs.pln[threadIdx.x];
-		S.lgt[threadIdx.x] = nullptr;
+		S.lvl[threadIdx.x] = S.edg[threadIdx.x] = nullptr;
 	}
 	__syncthreads();
 	mesh_chunk_cta(S, T, A, 0);
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_relight_single(Refs27 refs, Dev
 		S.blk[threadIdx.x] = refs.blk[threadIdx.x];
 		S.hgt[threadIdx.x] = refs.hgt[threadIdx.x];
 		S.pln[threadIdx.x] = refs.pln[threadIdx.x];
-		S.lgt[threadIdx.x] = nullptr;
+		S.lvl[threadIdx.x] = S.edg[threadIdx.x] = nullptr;
 	}
 	for (int i = threadIdx.x; i < 256; i += kThreads)
 		S.classes[i] = T.classes[i];
@@ -90,11 +90,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_relight_single(Refs27 refs, Dev
 enum : uint32_t { kChunkBadSlot = 2 };
 
 // Points S.blk / S.hgt at the 27 neighbour slots of batch item `item`; false if a slot is invalid.
-// With `light` (the batch light pass), S.lgt points at the 27 chunks' light, found through the batch's
-// own chunk numbering nbr_local.
+// With `levels` (the batch light pass), S.lvl / S.edg point at the 27 chunks' level planes and edge
+// bits, found through the batch's own chunk numbering nbr_local.
 __device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes,
-                          uint32_t pool_cap, const int32_t *nbr, uint32_t item, const uint8_t *light = nullptr,
-                          const int32_t *nbr_local = nullptr) {
+                          uint32_t pool_cap, const int32_t *nbr, uint32_t item, const uint32_t *levels = nullptr,
+                          const uint32_t *edges = nullptr, const int32_t *nbr_local = nullptr) {
 	__shared__ int s_bad;
 	if (threadIdx.x == 0)
 		s_bad = 0;
@@ -106,12 +106,14 @@ __device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *po
 			S.blk[threadIdx.x] = pool_blocks;
 			S.hgt[threadIdx.x] = pool_heights;
 			S.pln[threadIdx.x] = nullptr;
-			S.lgt[threadIdx.x] = nullptr;
+			S.lvl[threadIdx.x] = S.edg[threadIdx.x] = nullptr;
 		} else {
 			S.blk[threadIdx.x] = pool_blocks + (size_t)slot * 32768;
 			S.hgt[threadIdx.x] = pool_heights + (size_t)slot * 1024;
 			S.pln[threadIdx.x] = pool_planes ? pool_planes + (size_t)slot * kPlaneStride : nullptr;
-			S.lgt[threadIdx.x] = light ? light + (size_t)nbr_local[(size_t)item * 27 + threadIdx.x] * 32768 : nullptr;
+			const size_t loc = levels ? (size_t)nbr_local[(size_t)item * 27 + threadIdx.x] : 0;
+			S.lvl[threadIdx.x] = levels ? levels + loc * kLevelSlotWords : nullptr;
+			S.edg[threadIdx.x] = levels ? edges + loc * kEdgeSlotWords : nullptr;
 		}
 	}
 	__syncthreads();
@@ -157,7 +159,7 @@ __device__ __forceinline__ void prefetch_item(const uint16_t *pool_blocks, const
 __global__ void __launch_bounds__(kThreads, 1)
     k_mesh_batch(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
                  const int32_t *nbr, uint32_t n, const uint32_t *n_dev, unsigned int *work, unsigned int *failed,
-                 DevTables T, Arena A, const uint8_t *light, const int32_t *nbr_local) {
+                 DevTables T, Arena A, const uint32_t *levels, const uint32_t *edges, const int32_t *nbr_local) {
 	Smem &S = smem();
 	__shared__ uint32_t s_next;
 	if (n_dev) // the batch length is known on the device only (a world remesh)
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 		const uint32_t next = s_next;
 		if (next < n)
 			prefetch_item(pool_blocks, pool_planes, pool_cap, nbr, next);
-		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, light, nbr_local)) {
+		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, levels, edges, nbr_local)) {
 			mesh_chunk_cta(S, T, A, item);
 			if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
 				atomicAdd(failed, 1u);
@@ -193,8 +195,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 __global__ void __launch_bounds__(kThreads, 1)
     k_mesh_cluster(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes,
                    uint32_t pool_cap, const int32_t *nbr, uint32_t n, const uint32_t *n_dev, unsigned int *work,
-                   unsigned int *failed, DevTables T, Arena A, const uint8_t *light, const int32_t *nbr_local,
-                   int csize) {
+                   unsigned int *failed, DevTables T, Arena A, const uint32_t *levels, const uint32_t *edges,
+                   const int32_t *nbr_local, int csize) {
 	namespace cg = cooperative_groups;
 	cg::cluster_group cl = cg::this_cluster();
 	const int rank = (int)cl.block_rank();
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 		cl.sync(); // every CTA has read CTA 0's s_item: CTA 0 may now exit, or claim the next chunk
 		if (item >= n)
 			break;
-		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, light, nbr_local)) {
+		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, levels, edges, nbr_local)) {
 			mesh_chunk_cta(S, T, A, item, Split{csize, rank});
 			if (rank == 0 && threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
 				atomicAdd(failed, 1u);
@@ -314,7 +316,6 @@ struct hc_batch_plan {
 	int32_t *d_nbr_local = nullptr; // n x 27: the neighbour table in batch chunk numbers
 	uint32_t *d_levels = nullptr;   // per batch chunk: 2 channels x 15 level planes
 	uint32_t *d_edges = nullptr;    // per batch chunk: their x = 0 and x = 31 bits
-	uint8_t *d_light = nullptr;     // per batch chunk: 32768 light bytes
 	unsigned long long *d_state = nullptr; // quad cursor, mesh cursor, work counter, failed chunks
 	unsigned long long *h_state = nullptr; // pinned
 	cudaGraph_t graph = nullptr;
@@ -852,8 +853,6 @@ cudaError_t plan_light_tables(hc_batch_plan *p, const std::vector<int32_t> &tabl
 		e = cudaMalloc(&p->d_levels, (size_t)m * kLevelSlotWords * sizeof(uint32_t));
 	if (e == cudaSuccess)
 		e = cudaMalloc(&p->d_edges, (size_t)m * kEdgeSlotWords * sizeof(uint32_t));
-	if (e == cudaSuccess)
-		e = cudaMalloc(&p->d_light, (size_t)m * 32768);
 	return e;
 }
 
@@ -867,16 +866,13 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		                                     p->pool->d_planes);
 		HC_CUDA(ctx, cudaGetLastError());
 	}
-	if (p->d_light) {
-		const LightPass L{p->d_slots,  p->d_nb6,   p->pool->d_planes, p->pool->d_blocks,
-		                  p->d_levels, p->d_edges, p->d_light,        p->n_slots};
+	if (p->d_levels) {
+		const LightPass L{p->d_slots, p->d_nb6, p->pool->d_planes, p->pool->d_blocks, p->d_levels, p->d_edges, p->n_slots};
 		for (int t = kLevels; t >= 1; --t) {
 			k_light_level<<<p->n_slots, kLightThreads, 0, st>>>(L, tables(ctx), t);
 			HC_CUDA(ctx, cudaGetLastError());
 		}
-		const uint64_t rows = (uint64_t)p->n_slots * kPlaneWords;
-		k_light_bytes<<<(int)std::min<uint64_t>((rows + 255) / 256, (uint64_t)p->grid * 16), 256, 0, st>>>(L);
-		HC_CUDA(ctx, cudaGetLastError());
+
 	}
 	const Arena A = plan_arena(p);
 	unsigned int *work = reinterpret_cast<unsigned int *>(p->d_state + 2);
@@ -884,7 +880,8 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 	if (p->mode == HC_BATCH_PERSISTENT) {
 		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(p->pool->d_blocks, p->pool->d_heights, p->pool->d_planes,
 		                                                          p->pool->capacity, p->nbr, p->n, nullptr, work, failed,
-		                                                          tables(ctx), A, p->d_light, p->d_nbr_local);
+		                                                          tables(ctx), A, p->d_levels, p->d_edges,
+		                                                          p->d_nbr_local);
 		HC_CUDA(ctx, cudaGetLastError());
 	} else {
 		for (uint32_t i = 0; i < p->n; ++i) {
@@ -986,7 +983,6 @@ void hc_batch_plan_destroy(hc_batch_plan *plan) {
 	cudaFree(plan->d_nbr_local);
 	cudaFree(plan->d_levels);
 	cudaFree(plan->d_edges);
-	cudaFree(plan->d_light);
 	cudaFree(plan->d_state);
 	cudaFreeHost(plan->h_state);
 	delete plan;
@@ -1193,11 +1189,12 @@ hc_status world_enqueue_remesh(hc_world *w, const hc_batch_arena *arena, cudaStr
 		                                (const int8_t *)w->pool->d_heights, (const uint32_t *)w->pool->d_planes,
 		                                w->pool->capacity, (const int32_t *)w->d_nbr, 0u,
 		                                (const uint32_t *)(w->d_counts + kCountRemesh), work, failed, tables(ctx), A,
-		                                (const uint8_t *)nullptr, (const int32_t *)nullptr, w->cluster));
+		                                (const uint32_t *)nullptr, (const uint32_t *)nullptr, (const int32_t *)nullptr,
+		                                w->cluster));
 	} else {
 		k_mesh_batch<<<w->sms, kThreads, ctx->smem_bytes, st>>>(
 		    w->pool->d_blocks, w->pool->d_heights, w->pool->d_planes, w->pool->capacity, w->d_nbr, 0u,
-		    w->d_counts + kCountRemesh, work, failed, tables(ctx), A, nullptr, nullptr);
+		    w->d_counts + kCountRemesh, work, failed, tables(ctx), A, nullptr, nullptr, nullptr);
 	}
 	HC_CUDA(ctx, cudaGetLastError());
 	k_requeue<<<list_grid(w), 256, 0, st>>>(W, w->d_list, A.results);
@@ -1730,7 +1727,7 @@ extern "C" hc_status hc_mesh_batch_noalloc(const uint16_t *pool_blocks, const in
 		        results};
 		k_mesh_batch<<<D.sms, kThreads, sizeof(Smem), st>>>(pool_blocks, pool_heights, nullptr, pool_capacity, neighbours,
 		                                                     n, nullptr, state + 4, state + 5, DevTables{D.class_of, D.classes}, A,
-		                                                     nullptr, nullptr);
+		                                                     nullptr, nullptr, nullptr);
 		e = cudaGetLastError();
 	}
 	uint32_t host_state[kNoAllocStateWords];

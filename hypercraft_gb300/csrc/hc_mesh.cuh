@@ -24,15 +24,6 @@
 
 namespace hc {
 
-// How the face planes of one chunk are shared by the CTAs of a thread-block cluster (a chunk
-// meshed by several SMs, for latency): CTA `rank` of `c` owns the slices axis * 33 + slice that
-// are congruent to rank mod c, with both face directions of each. Every CTA stages the whole chunk.
-struct Split {
-	int c, rank;
-	__device__ __forceinline__ int planes() const { return 2 * ((kSlices - rank + c - 1) / c); }
-	__device__ __forceinline__ int plane(int j) const { return 2 * (rank + c * (j >> 1)) + (j & 1); }
-	__device__ __forceinline__ int owner(int p) const { return (p >> 1) % c; }
-};
 
 // Next index of a per-plane phase for the calling warp (all lanes get it): warps take planes as
 // they finish the previous one, so a phase ends when the work does, not when the unluckiest warp's
@@ -43,7 +34,27 @@ __device__ __forceinline__ int claim(uint32_t *counter) {
 		j = (int)atomicAdd(counter, 1u);
 	return __shfl_sync(0xffffffffu, j, 0);
 }
-enum : int { kClaimComplex = 12, kClaimKeys = 13, kClaimCount = 14 }; // S.misc counters
+enum : int { kClaimComplex = 12, kClaimKeys = 13, kClaimCount = 14, kMine = 15 }; // S.misc counters
+
+// Next face plane for the calling warp's key pass. In a cluster the planes are taken from one
+// counter in CTA 0, so a heavy plane does not hold up a CTA with a fixed share; the taker records
+// the plane as its own (count and emission run where its masks are) and in CTA 0's owner table.
+__device__ __forceinline__ int claim_plane(Smem &S, const Split &sp) {
+	int p = 0;
+	if ((threadIdx.x & 31) == 0) {
+		if (sp.c > 1) {
+			cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+			p = (int)atomicAdd(cl.map_shared_rank(&S.misc[kClaimKeys], 0), 1u);
+			if (p < kPlanes)
+				cl.map_shared_rank(&S.plane_owner[0], 0)[p] = (uint8_t)sp.rank;
+		} else {
+			p = (int)atomicAdd(&S.misc[kClaimKeys], 1u);
+		}
+		if (p < kPlanes)
+			S.mine[atomicAdd(&S.misc[kMine], 1u)] = (uint8_t)p;
+	}
+	return __shfl_sync(0xffffffffu, p, 0);
+}
 
 struct Emit {
 	uint2 *verts;
@@ -362,38 +373,37 @@ __device__ void plane_visibility(Smem &S) {
 	}
 }
 
-// Pass 1b: exact Show for the complex candidates of every plane row (texture lookups, dynamic
-// liquid textures), and transparent-pass bits of the faces it shows. Lane = plane row.
-__device__ void plane_complex(Smem &S, const Split &sp) {
+// Pass 1b: exact Show for the complex candidates of one plane's rows (texture lookups, dynamic
+// liquid textures), and transparent-pass bits of the faces it shows. Lane = plane row. Run by the
+// warp that takes the plane for its keys.
+__device__ __forceinline__ void plane_complex_one(Smem &S, int p) {
 	const int lane = threadIdx.x & 31;
-	for (int j = claim(&S.misc[kClaimComplex]); j < sp.planes(); j = claim(&S.misc[kClaimComplex])) {
-		const int p = sp.plane(j);
-		uint32_t *m = S.u.masks[p][lane];
-		uint32_t cx = m[1];
-		if (!__any_sync(0xffffffffu, cx != 0))
-			continue;
-		const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
-		uint32_t vis = m[0], tp = 0;
-		while (cx) {
-			const int v = __ffs(cx) - 1;
-			cx &= cx - 1;
-			int x, y, z;
-			to_xyz(a, s, lane, v, x, y, z);
-			int nx = x, ny = y, nz = z;
-			(a == 0 ? nx : (a == 1 ? ny : nz)) -= 1;
-			const uint16_t ta = get_tex(S, nx, ny, nz, 2 * a), tb = get_tex(S, x, y, z, 2 * a + 1);
-			const uint16_t mine = inv ? tb : ta, other = inv ? ta : tb;
-			if (show(mine, other)) {
-				vis |= 1u << v;
-				if (tex_transpass(mine))
-					tp |= 1u << v;
-			} else {
-				vis &= ~(1u << v);
-			}
+	uint32_t *m = S.u.masks[p][lane];
+	uint32_t cx = m[1];
+	if (!__any_sync(0xffffffffu, cx != 0))
+		return;
+	const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
+	uint32_t vis = m[0], tp = 0;
+	while (cx) {
+		const int v = __ffs(cx) - 1;
+		cx &= cx - 1;
+		int x, y, z;
+		to_xyz(a, s, lane, v, x, y, z);
+		int nx = x, ny = y, nz = z;
+		(a == 0 ? nx : (a == 1 ? ny : nz)) -= 1;
+		const uint16_t ta = get_tex(S, nx, ny, nz, 2 * a), tb = get_tex(S, x, y, z, 2 * a + 1);
+		const uint16_t mine = inv ? tb : ta, other = inv ? ta : tb;
+		if (show(mine, other)) {
+			vis |= 1u << v;
+			if (tex_transpass(mine))
+				tp |= 1u << v;
+		} else {
+			vis &= ~(1u << v);
 		}
-		m[0] = vis;
-		m[3] = tp;
 	}
+	m[0] = vis;
+	m[3] = tp;
+	__syncwarp();
 }
 
 // Position of the n-th (0-based) set bit of mask (n < popc(mask)), by halving the search window.
@@ -446,8 +456,8 @@ __device__ __forceinline__ Key face_key(const Smem &S, int a, int s, int inv, in
 // upper neighbour sits in this batch or in the previous one.
 __device__ void plane_keys(Smem &S, const Split &sp) {
 	const int lane = threadIdx.x & 31;
-	for (int j = claim(&S.misc[kClaimKeys]); j < sp.planes(); j = claim(&S.misc[kClaimKeys])) {
-		const int p = sp.plane(j);
+	for (int p = claim_plane(S, sp); p < kPlanes; p = claim_plane(S, sp)) {
+		plane_complex_one(S, p);
 		uint32_t *mrow = S.u.masks[p][lane];
 		const uint32_t N = mrow[0];
 		mrow[1] = 0;
@@ -573,8 +583,9 @@ __device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, 
 __device__ void planes_count(Smem &S, const Split &sp) {
 	const int lane = threadIdx.x & 31;
 	const uint32_t lt = (1u << lane) - 1u;
-	for (int j = claim(&S.misc[kClaimCount]); j < sp.planes(); j = claim(&S.misc[kClaimCount])) {
-		const int p = sp.plane(j);
+	const int n_mine = (int)S.misc[kMine];
+	for (int j = claim(&S.misc[kClaimCount]); j < n_mine; j = claim(&S.misc[kClaimCount])) {
+		const int p = S.mine[j];
 		uint32_t n_all = 0, n_st[2] = {0, 0};
 		warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
 			const uint32_t cnt = __popc(starts);
@@ -645,9 +656,10 @@ __device__ __forceinline__ void emit_record(Smem &S, const Emit &E, bool valid, 
 }
 
 // Emits the plane quads this CTA owns. Normally planes_count kept all their records; otherwise
-// the quads are taken in windows of kQuadBuf (in output order), the planes overlapping a window
-// merge again to stage that window's records, and the whole CTA writes them. Emission of a window
-// is spread over every thread: a heavy plane does not wait on the warp that merges it.
+// this CTA's quads are taken in windows of kQuadBuf (its planes in the order it took them, each
+// plane's quads in order), the planes overlapping a window merge again to stage that window's
+// records, and the whole CTA writes them. Emission of a window is spread over every thread: a
+// heavy plane does not wait on the warp that merges it.
 __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	if (!S.misc[5]) {
@@ -658,19 +670,36 @@ __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 		}
 		return;
 	}
-	const uint32_t lt = (1u << lane) - 1u;
-	const uint32_t custom_all = S.seg_base[2][1];
-	const uint32_t plane_quads = S.misc[0] + S.misc[1] - custom_all;
-	for (uint32_t w0 = 0; w0 < plane_quads; w0 += kQuadBuf) {
-		if (sp.c > 1) { // other CTAs' quads of this window stay unfilled here
-			for (int j = tid; j < kQuadBuf; j += kThreads)
-				S.aux.quads[j].x = 0xffffffffu;
-			__syncthreads();
+	// own-quad offset of each taken plane (one warp; up to kPlanes entries)
+	const int n_mine = (int)S.misc[kMine];
+	__shared__ uint32_t s_obase[kPlanes + 1];
+	if (warp == 0) {
+		uint32_t run = 0;
+		for (int j0 = 0; j0 < n_mine; j0 += 32) {
+			const int j = j0 + lane;
+			const int p = j < n_mine ? S.mine[j] : 0;
+			const uint32_t c = j < n_mine ? S.seg_cnt[0][1 + p] + S.seg_cnt[1][1 + p] : 0u;
+			uint32_t incl = c;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+				if (lane >= d)
+					incl += o;
+			}
+			if (j < n_mine)
+				s_obase[j] = run + incl - c;
+			run += __shfl_sync(0xffffffffu, incl, 31);
 		}
-		for (int jp = warp; jp < sp.planes(); jp += kWarps) {
-			const int p = sp.plane(jp);
-			const uint32_t pb = S.seg_base[2][1 + p] - custom_all;
-			const uint32_t pc = S.seg_cnt[0][1 + p] + S.seg_cnt[1][1 + p];
+		if (lane == 0)
+			s_obase[n_mine] = run;
+	}
+	__syncthreads();
+	const uint32_t lt = (1u << lane) - 1u;
+	const uint32_t own_quads = s_obase[n_mine];
+	for (uint32_t w0 = 0; w0 < own_quads; w0 += kQuadBuf) {
+		for (int jp = warp; jp < n_mine; jp += kWarps) {
+			const int p = S.mine[jp];
+			const uint32_t pb = s_obase[jp], pc = s_obase[jp + 1] - pb;
 			if (!pc || pb >= w0 + kQuadBuf || pb + pc <= w0)
 				continue;
 			uint32_t n_all = 0, n_st[2] = {0, 0};
@@ -689,11 +718,10 @@ __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 			});
 		}
 		__syncthreads();
-		const uint32_t n = min((uint32_t)kQuadBuf, plane_quads - w0);
+		const uint32_t n = min((uint32_t)kQuadBuf, own_quads - w0);
 		for (uint32_t j0 = (uint32_t)warp * 32; j0 < n; j0 += kThreads) {
 			const uint32_t j = j0 + lane;
-			const bool valid = j < n && S.aux.quads[j].x != 0xffffffffu;
-			emit_record(S, E, valid, valid ? S.aux.quads[j] : make_uint2(0, 0));
+			emit_record(S, E, j < n, j < n ? S.aux.quads[j] : make_uint2(0, 0));
 		}
 		__syncthreads();
 	}
@@ -788,7 +816,7 @@ struct Arena {
 enum : uint32_t { kChunkOk = 0, kChunkCapacity = 1 };
 
 // Relights and meshes one chunk whose 27 neighbour pointers are already in S.blk / S.hgt / S.pln
-// (and S.lgt). With sp.c > 1 the c CTAs of a cluster mesh it together: each stages it, owns a
+// (and S.lvl / S.edg). With sp.c > 1 the c CTAs of a cluster mesh it together: each stages it, owns a
 // share of the face planes, and they exchange per-plane counts, the arena reservation and the
 // meshes' bounding boxes through distributed shared memory; CTA 0 writes the results and the
 // mesh descriptors. Every CTA of the cluster must call this with the same chunk.
@@ -804,8 +832,9 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 	}
 	for (int i = tid; i < 2 * (kSegments + 1); i += kThreads)
 		S.seg_cnt[i / (kSegments + 1)][i % (kSegments + 1)] = 0;
-	if (tid < 3)
-		S.misc[kClaimComplex + tid] = 0; // the stage's barriers order this before the plane phases
+	if (tid < 4)
+		S.misc[kClaimComplex + tid] = 0; // the stage's barriers (and, in a cluster, the relight's) order
+	                                     // this before any CTA's plane phases
 	const bool blank = stage_classes(S, T);
 
 	uint32_t qo = 0, qt = 0;
@@ -815,15 +844,15 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		if (lead)
 			custom_count(S, tid * kBlocksPerThread, co, ct);
 		block_scan2(S, co, ct, eo, et, to, tt);
-		if (S.lgt[26])
-			light_from_batch(S);
+		if (S.lvl[26])
+			light_from_levels(S);
 		else
-			relight_window(S, T); // the relight scratch shares memory with the plane masks
+			relight_window(S, T, sp); // the relight scratch shares memory with the plane masks
 		__syncthreads();
 		plane_visibility(S);
 		__syncthreads();
-		plane_complex(S, sp);
-		__syncthreads();
+		if (sp.c > 1) // CTA 0's plane counter was reset for this chunk before any CTA takes from it
+			cooperative_groups::this_cluster().sync();
 		plane_keys(S, sp);
 		if (tid == 0) {
 			S.seg_cnt[0][0] = to;
@@ -838,7 +867,7 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 			cg::cluster_group cl = cg::this_cluster();
 			cl.sync();
 			for (int i = tid; i < kSegments; i += kThreads) {
-				const int owner = i == 0 ? 0 : sp.owner(i - 1);
+				const int owner = i == 0 ? 0 : cl.map_shared_rank(&S.plane_owner[0], 0)[i - 1];
 				if (owner != sp.rank) {
 					const uint32_t *src = cl.map_shared_rank(&S.seg_cnt[0][0], owner);
 					S.seg_cnt[0][i] = src[i];

@@ -12,9 +12,29 @@
 // so fourteen 6-neighbour dilations of 62-bit row masks give every level exactly. A cell's light
 // is the largest t with the cell in S_t. Only [-1, 32]^3 (what the mesher reads) is written out.
 #pragma once
+#include <cooperative_groups.h>
+
 #include "hc_device.cuh"
 
 namespace hc {
+
+// How one chunk's work is shared by the CTAs of a thread-block cluster (a chunk meshed by several
+// SMs, for latency). Face planes: CTA `rank` of `c` owns the slices axis * 33 + slice that are
+// congruent to rank mod c, with both face directions of each. Relight window: CTA `rank` owns
+// the window rows y in [rank * 62 / c, (rank + 1) * 62 / c). Every CTA stages the whole chunk.
+struct Split {
+	int c, rank;
+	__device__ __forceinline__ int planes() const { return 2 * ((kSlices - rank + c - 1) / c); }
+	__device__ __forceinline__ int plane(int j) const { return 2 * (rank + c * (j >> 1)) + (j & 1); }
+	__device__ __forceinline__ int owner(int p) const { return (p >> 1) % c; }
+	__device__ __forceinline__ int win_lo(int r) const { return r * kWin / c; }
+	__device__ __forceinline__ int win_owner(int wy) const {
+		int r = 0;
+		while (r + 1 < c && win_lo(r + 1) <= wy)
+			++r;
+		return r;
+	}
+};
 
 // Distance of one coordinate to [-1, 33) as IsBorderLightInterfere computes it.
 __device__ __forceinline__ int axis_dist(int v) { return v < -1 ? -1 - v : (v >= 33 ? v - 33 : 0); }
@@ -55,9 +75,9 @@ __device__ __forceinline__ void write_row15(uint8_t *light, int wy, int wz, uint
 }
 
 // Seeds from the 27 chunks' bit planes: each window row joins three 32-bit chunk rows.
-__device__ void seed_from_planes(Smem &S) {
+__device__ void seed_from_planes(Smem &S, int r_lo, int r_hi) {
 	Relight &R = S.u.rl;
-	for (int r = threadIdx.x; r < kWinRows; r += kThreads) {
+	for (int r = r_lo + threadIdx.x; r < r_hi; r += kThreads) {
 		const int wy = r / kWin, wz = r - wy * kWin, y = wy - 15, z = wz - 15;
 		const int prow = (z & 31) + 32 * (y & 31);
 		uint32_t w[3][3], low = 0;
@@ -82,10 +102,10 @@ __device__ void seed_from_planes(Smem &S) {
 }
 
 // Seeds from the blocks themselves (used when no planes are given), one warp per row.
-__device__ void seed_from_blocks(Smem &S, const DevTables &T) {
+__device__ void seed_from_blocks(Smem &S, const DevTables &T, int r_lo, int r_hi) {
 	Relight &R = S.u.rl;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int r = warp; r < kWinRows; r += kWarps) {
+	for (int r = r_lo + warp; r < r_hi; r += kWarps) {
 		const int wy = r / kWin, wz = r - wy * kWin, y = wy - 15, z = wz - 15;
 		uint64_t pass = 0, sun = 0, torch = 0;
 		bool low = false;
@@ -113,7 +133,7 @@ __device__ void seed_from_blocks(Smem &S, const DevTables &T) {
 		}
 	}
 	__syncthreads();
-	for (int r = threadIdx.x; r < kWinRows; r += kThreads) {
+	for (int r = r_lo + threadIdx.x; r < r_hi; r += kThreads) {
 		const int wy = r / kWin, wz = r - wy * kWin;
 		const ulonglong2 l = R.lit[r];
 		write_row15(light_bytes(S), wy, wz, l.x, l.y);
@@ -123,16 +143,26 @@ __device__ void seed_from_blocks(Smem &S, const DevTables &T) {
 // Bit of row r in a row bitmap.
 __device__ __forceinline__ bool row_bit(const uint32_t *m, int r) { return (m[r >> 5] >> (r & 31)) & 1u; }
 
-__device__ void relight_window(Smem &S, const DevTables &T) {
+// With sp.c > 1 the CTAs of a cluster share the window by rows (Split::win_lo): each seeds its
+// rows and the row next to them on either side, runs the cascade on its own rows, and after every
+// level takes the two neighbouring rows from the CTAs that own them (distributed shared memory);
+// at the end each takes the light of [-1, 32]^3 the others computed. Every CTA of the cluster
+// passes the same cluster barriers.
+__device__ void relight_window(Smem &S, const DevTables &T, const Split &sp = Split{1, 0}) {
+	namespace cg = cooperative_groups;
 	Relight &R = S.u.rl;
 	const int tid = threadIdx.x;
+	const bool split = sp.c > 1;
+	const int wlo = split ? sp.win_lo(sp.rank) : 0, whi = split ? sp.win_lo(sp.rank + 1) : kWin;
+	const int seed_lo = (wlo > 0 ? wlo - 1 : 0) * kWin, seed_hi = (whi < kWin ? whi + 1 : kWin) * kWin;
+	const int own_lo = wlo * kWin, own_hi = whi * kWin;
 	for (int i = tid; i < kRowWords; i += kThreads)
 		R.low_rows[i] = 0, R.changed[0][i] = 0, R.changed[1][i] = 0;
 	__syncthreads();
 	if (S.pln[26])
-		seed_from_planes(S);
+		seed_from_planes(S, seed_lo, seed_hi);
 	else
-		seed_from_blocks(S, T);
+		seed_from_blocks(S, T, seed_lo, seed_hi);
 	__syncthreads();
 
 	// A row can gain cells at level t only when it or one of its four neighbour rows changed at
@@ -143,9 +173,9 @@ __device__ void relight_window(Smem &S, const DevTables &T) {
 	int rem0[kRowsPerThread]; // t - 1 - dist(y, z) = t + rem0
 #pragma unroll
 	for (int k = 0; k < kRowsPerThread; ++k) {
-		const int r = tid + k * kThreads;
+		const int r = own_lo + tid + k * kThreads;
 		const int wy = r / kWin, wz = r - wy * kWin;
-		rem0[k] = r < kWinRows ? -1 - axis_dist(wy - 15) - axis_dist(wz - 15) : -1000;
+		rem0[k] = r < own_hi ? -1 - axis_dist(wy - 15) - axis_dist(wz - 15) : -1000;
 	}
 	uint8_t *light = light_bytes(S);
 	for (int t = 14; t >= 1; --t) {
@@ -157,15 +187,15 @@ __device__ void relight_window(Smem &S, const DevTables &T) {
 		uint32_t changed = 0;
 #pragma unroll
 		for (int k = 0; k < kRowsPerThread; ++k) {
-			const int r = tid + k * kThreads;
+			const int r = own_lo + tid + k * kThreads;
 			const int rem = t + rem0[k];
-			if (r >= kWinRows)
+			if (r >= own_hi)
 				continue;
 			const bool low = row_bit(R.low_rows, r);
 			if (rem < 0 && !low)
 				continue;
 			const int wy = r / kWin, wz = r - wy * kWin;
-			if (t < 14 && !low) {
+			if (t < 14 && !low && !split) { // (split: the neighbour rows' changes are not tracked)
 				const bool near = row_bit(prev, r) || (wz > 0 && row_bit(prev, r - 1)) ||
 				                  (wz < kWin - 1 && row_bit(prev, r + 1)) || (wy > 0 && row_bit(prev, r - kWin)) ||
 				                  (wy < kWin - 1 && row_bit(prev, r + kWin));
@@ -215,13 +245,33 @@ __device__ void relight_window(Smem &S, const DevTables &T) {
 		for (int k = 0; k < kRowsPerThread; ++k) {
 			if (!((changed >> k) & 1u))
 				continue;
-			const int r = tid + k * kThreads;
+			const int r = own_lo + tid + k * kThreads;
 			const int wy = r / kWin, wz = r - wy * kWin;
 			const ulonglong2 cur = R.lit[r];
 			R.lit[r] = make_ulonglong2(ns[k], nt[k]);
 			atomicOr(&cur_chg[r >> 5], 1u << (r & 31));
 			write_new(light, wy, wz, ns[k] & ~cur.x, (uint32_t)t, 0);
 			write_new(light, wy, wz, nt[k] & ~cur.y, (uint32_t)t, 4);
+		}
+		__syncthreads();
+		if (split) { // the rows next to this CTA's, as their owners left them at this level
+			cg::cluster_group cl = cg::this_cluster();
+			cl.sync();
+			for (int i = tid; i < 2 * kWin; i += kThreads) {
+				const int side = i / kWin, wz = i - side * kWin, wy = side ? whi : wlo - 1;
+				if (wy >= 0 && wy < kWin)
+					R.lit[wy * kWin + wz] = cl.map_shared_rank(&R.lit[0], sp.rank + (side ? 1 : -1))[wy * kWin + wz];
+			}
+			cl.sync();
+		}
+	}
+	if (split) { // light of [-1, 32]^3 rows other CTAs own
+		cg::cluster_group cl = cg::this_cluster();
+		for (int i = tid; i < kLtCells; i += kThreads) {
+			const int wy = i / (kLt * kLt) + 14;
+			if (wy >= wlo && wy < whi)
+				continue;
+			light[2 * i] = (uint8_t)(cl.map_shared_rank(&S.cell[0], sp.win_owner(wy))[i] & 0xffu);
 		}
 		__syncthreads();
 	}
@@ -331,7 +381,6 @@ struct LightPass {
 	const uint16_t *blocks; // pool blocks (rows with emitters below 15)
 	uint32_t *levels;       // batch chunk -> channel -> level t at plane t - 1 -> 1024 rows
 	uint32_t *edges;        // batch chunk -> channel -> level -> {bit x = 0, bit x = 31} of every row
-	uint8_t *light;         // batch chunk -> 32768 cells (sun | torch << 4), the reference's cell order
 	uint32_t n;             // batch chunks
 };
 
@@ -459,60 +508,57 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 	}
 }
 
-// Light bytes of every cell of every batch chunk from its 15 level planes per channel (one thread
-// per row, a streaming pass).
-__global__ void __launch_bounds__(256) k_light_bytes(LightPass L) {
-	const uint64_t total = (uint64_t)L.n * kPlaneWords;
-	for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (uint64_t)gridDim.x * blockDim.x) {
-		const int i = (int)(g >> 10), r = (int)(g & 1023u);
+// Light of [-1, 32]^3 from the batch light pass (instead of relight_window), decoded from the 15
+// nested level planes per channel into the low byte of every staged cell: a cell's light is the
+// number of levels that hold it, read as four binary digits by level_bits. Cells x in [0, 32) of
+// each row come from the level words of the row's chunk; x = -1 and x = 32 from the x neighbours'
+// edge bits, 32 rows (z) per word.
+__device__ void light_from_levels(Smem &S) {
+	uint8_t *light = light_bytes(S);
+	for (int row = threadIdx.x; row < kLt * kLt; row += kThreads) {
+		const int y = row / kLt - 1, z = row % kLt - 1;
+		const uint32_t *L = S.lvl[nb_index(0, y, z)];
+		const int ry = (y & 31) * 32 + (z & 31);
 		uint32_t b[2][4];
 #pragma unroll
 		for (int c = 0; c < 2; ++c) {
 			uint32_t lv[kLevels];
 #pragma unroll
-			for (int u = 1; u <= kLevels; ++u)
-				lv[u - 1] = __ldg(level_plane(L, i, c, u) + r);
+			for (int u = 0; u < kLevels; ++u)
+				lv[u] = __ldg(L + (size_t)(c * kLevels + u) * kPlaneWords + ry);
 			level_bits(lv, b[c]);
 		}
-		uint32_t w[8];
-#pragma unroll
-		for (int q = 0; q < 8; ++q) {
-			uint32_t val = 0;
-#pragma unroll
-			for (int kk = 0; kk < 4; ++kk) {
-				const int x = 4 * q + kk;
-				uint32_t byte = 0;
-#pragma unroll
-				for (int bit = 0; bit < 4; ++bit)
-					byte |= ((b[0][bit] >> x) & 1u) << bit | ((b[1][bit] >> x) & 1u) << (bit + 4);
-				val |= byte << (8 * kk);
-			}
-			w[q] = val;
-		}
-		uint4 *dst = reinterpret_cast<uint4 *>(L.light + (size_t)i * 32768 + r * 32);
-		dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
-		dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
-	}
-}
-
-// Light of [-1, 32]^3 from the batch light pass (instead of relight_window): the chunk's own rows
-// and the neighbours' edge cells, into the low byte of every staged cell.
-__device__ void light_from_batch(Smem &S) {
-	uint8_t *light = light_bytes(S);
-	for (int k = threadIdx.x; k < kLt * kLt * 10; k += kThreads) {
-		const int row = k / 10, part = k - row * 10;
-		const int y = row / kLt - 1, z = row % kLt - 1;
 		uint8_t *dst = light + 2 * (row * kLt + 1); // cell x = 0 of the row
-		const int in = ((y & 31) * 32 + (z & 31)) * 32;
-		if (part < 8) {
-			const uint32_t v = *reinterpret_cast<const uint32_t *>(S.lgt[nb_index(0, y, z)] + in + 4 * part);
+#pragma unroll 8
+		for (int x = 0; x < 32; ++x) {
+			uint32_t v = 0;
 #pragma unroll
-			for (int b = 0; b < 4; ++b)
-				dst[2 * (4 * part + b)] = (uint8_t)(v >> (8 * b));
-		} else if (part == 8) {
-			dst[-2] = S.lgt[nb_index(-1, y, z)][in + 31];
-		} else {
-			dst[2 * 32] = S.lgt[nb_index(32, y, z)][in];
+			for (int bit = 0; bit < 4; ++bit)
+				v |= ((b[0][bit] >> x) & 1u) << bit | ((b[1][bit] >> x) & 1u) << (bit + 4);
+			dst[2 * x] = (uint8_t)v;
+		}
+	}
+	for (int k = threadIdx.x; k < 2 * kLt * 3; k += kThreads) {
+		const int side = k / (kLt * 3), rem = k - side * (kLt * 3), y = rem / 3 - 1, zc = rem % 3;
+		const int x = side ? kChunk : -1, z0 = zc == 0 ? -1 : (zc == 1 ? 0 : kChunk);
+		const uint32_t *E = S.edg[nb_index(x, y, z0)] + (side ? 0 : 32) + (y & 31); // x = 0 or x = 31 bits
+		uint32_t b[2][4];
+#pragma unroll
+		for (int c = 0; c < 2; ++c) {
+			uint32_t lv[kLevels];
+#pragma unroll
+			for (int u = 0; u < kLevels; ++u)
+				lv[u] = __ldg(E + (size_t)(c * kLevels + u) * 64);
+			level_bits(lv, b[c]);
+		}
+		const int zlo = zc == 1 ? 0 : z0, zhi = zc == 1 ? kChunk : z0 + 1;
+		for (int z = zlo; z < zhi; ++z) {
+			const int bz = z & 31;
+			uint32_t v = 0;
+#pragma unroll
+			for (int bit = 0; bit < 4; ++bit)
+				v |= ((b[0][bit] >> bz) & 1u) << bit | ((b[1][bit] >> bz) & 1u) << (bit + 4);
+			light[2 * lt_index(x, y, z)] = (uint8_t)v;
 		}
 	}
 }
