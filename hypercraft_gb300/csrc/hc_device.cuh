@@ -111,6 +111,7 @@ struct Relight {
 struct Smem {
 	DevClass classes[256];
 	uint8_t cflags[256]; // classes[c].flags, packed (fewer bank conflicts when lanes look up many classes)
+	uint32_t cmesh[8];   // the classes with a custom mesh, as a 256-bit set
 	const uint16_t *blk[27];
 	const int8_t *hgt[27];
 	const uint32_t *pln[27]; // per-chunk bit planes, or null (then the window is seeded from blocks)

@@ -125,7 +125,7 @@ __device__ __forceinline__ void put_quad(Smem &S, const Emit &E, int st, uint32_
 // flight), and builds the x-row bit planes of opaque full cubes and of blank blocks. Returns true
 // when the chunk can produce no quad: every inner block has no texture and no custom mesh, or every
 // inner block and every block of the six adjacent layers is an opaque full cube.
-__device__ bool stage_classes(Smem &S, const DevTables &T) {
+__device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 	// With the planes, the chunk's own 32 KB of class ids are copied into the plane-mask scratch
 	// (unused until the light and plane passes) by asynchronous 16-byte copies, all in flight at
 	// once; the apron's class ids come straight from the neighbours' planes.
@@ -141,24 +141,68 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 		const DevClass k = T.classes[i];
 		S.classes[i] = k;
 		S.cflags[i] = k.flags;
+		// classes with a custom mesh, as a 256-bit set
+		const uint32_t cm = __ballot_sync(0xffffffffu, (k.mesh_meta & 3u) != 0);
+		if ((threadIdx.x & 31) == 0)
+			S.cmesh[i >> 5] = cm;
 	}
 	if (S.pln[26])
 		asm volatile("cp.async.wait_group 0;" ::: "memory");
 	__syncthreads();
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	constexpr int kRows = kCls * kCls, kBatch = 12; // 1156 rows; 12 in flight per warp
-	bool content = false, open = false;
-	for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
-		uint8_t c[kBatch], ce[kBatch];
-		if (S.pln[26]) { // class ids precomputed with the planes
+	bool content = false, open = false, custom = false;
+	if (S.pln[26]) {
+		// class ids of the x = -1 and x = 32 cells of every row, gathered once (one thread each)
+		uint8_t *edge = reinterpret_cast<uint8_t *>(&S.u) + 32768; // [2][kRows], past the own ids
+		for (int i = threadIdx.x; i < 2 * kRows; i += kThreads) {
+			const int side = i / kRows, row = i - side * kRows, y = row / kCls - 1, z = row % kCls - 1;
+			edge[i] = class_byte(S, side ? kChunk : -1, y, z);
+		}
+		__syncthreads();
+		for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
+			uint8_t c[kBatch];
 #pragma unroll
 			for (int j = 0; j < kBatch; ++j) {
 				const int row = min(row0 + j, kRows - 1), y = row / kCls - 1, z = row % kCls - 1;
 				const bool inner = (unsigned)y < (unsigned)kChunk && (unsigned)z < (unsigned)kChunk;
 				c[j] = inner ? own[lane + (y * kChunk + z) * kChunk] : class_byte(S, lane, y, z);
-				ce[j] = lane < 2 ? class_byte(S, lane ? kChunk : -1, y, z) : (uint8_t)0;
 			}
-		} else {
+#pragma unroll
+			for (int j = 0; j < kBatch; ++j) {
+				const int row = row0 + j, y = row / kCls - 1, z = row % kCls - 1;
+				if (row >= kRows) // the same for the whole warp
+					break;
+				uint16_t *dst = S.cell + row * kCls;
+				dst[lane + 1] = (uint16_t)(c[j] << 8);
+				const uint8_t f = S.cflags[c[j]];
+				const uint32_t oc = __ballot_sync(0xffffffffu, f & kFOpaqueCube);
+				const uint32_t em = __ballot_sync(0xffffffffu, f & kFEmpty);
+				const bool yin = (unsigned)y < (unsigned)kChunk, zin = (unsigned)z < (unsigned)kChunk;
+				if (lane == 0) { // the two edge cells of the row
+					const uint8_t e0 = edge[row], e1 = edge[kRows + row];
+					dst[0] = (uint16_t)(e0 << 8);
+					dst[kCls - 1] = (uint16_t)(e1 << 8);
+					const uint8_t f0 = S.cflags[e0], f1 = S.cflags[e1];
+					S.aux.pl.oc[row] = (uint64_t)((f0 & kFOpaqueCube) != 0) | ((uint64_t)oc << 1) |
+					                   ((uint64_t)((f1 & kFOpaqueCube) != 0) << 33);
+					S.aux.pl.em[row] = (uint64_t)((f0 & kFEmpty) != 0) | ((uint64_t)em << 1) |
+					                   ((uint64_t)((f1 & kFEmpty) != 0) << 33);
+					if (yin && zin)
+						open |= !(f0 & kFOpaqueCube) || !(f1 & kFOpaqueCube);
+				}
+				if (yin && zin) {
+					content |= !(f & kFEmpty);
+					open |= !(f & kFOpaqueCube);
+					custom |= (S.cmesh[c[j] >> 5] >> (c[j] & 31)) & 1u;
+				} else if (yin || zin) { // a face-adjacent layer row (x in [0, 32))
+					open |= !(f & kFOpaqueCube);
+				}
+			}
+		}
+	} else {
+		for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
+			uint8_t c[kBatch], ce[kBatch];
 			uint16_t raw[kBatch], rawe[kBatch];
 #pragma unroll
 			for (int j = 0; j < kBatch; ++j) {
@@ -171,36 +215,38 @@ __device__ bool stage_classes(Smem &S, const DevTables &T) {
 				c[j] = __ldg(T.class_of + raw[j]);
 				ce[j] = __ldg(T.class_of + rawe[j]);
 			}
-		}
 #pragma unroll
-		for (int j = 0; j < kBatch; ++j) {
-			const int row = row0 + j, y = row / kCls - 1, z = row % kCls - 1;
-			if (row >= kRows) // the same for the whole warp
-				break;
-			uint16_t *dst = S.cell + row * kCls;
-			dst[lane + 1] = (uint16_t)(c[j] << 8);
-			if (lane < 2)
-				dst[lane ? kCls - 1 : 0] = (uint16_t)(ce[j] << 8);
-			const uint8_t f = S.cflags[c[j]], fe = S.cflags[ce[j]];
-			const uint32_t oc = __ballot_sync(0xffffffffu, f & kFOpaqueCube);
-			const uint32_t em = __ballot_sync(0xffffffffu, f & kFEmpty);
-			const uint32_t oce = __ballot_sync(0xffffffffu, lane < 2 && (fe & kFOpaqueCube));
-			const uint32_t eme = __ballot_sync(0xffffffffu, lane < 2 && (fe & kFEmpty));
-			if (lane == 0) {
-				S.aux.pl.oc[row] = (uint64_t)(oce & 1u) | ((uint64_t)oc << 1) | ((uint64_t)((oce >> 1) & 1u) << 33);
-				S.aux.pl.em[row] = (uint64_t)(eme & 1u) | ((uint64_t)em << 1) | ((uint64_t)((eme >> 1) & 1u) << 33);
-			}
-			const bool yin = y >= 0 && y < kChunk, zin = z >= 0 && z < kChunk;
-			if (yin && zin) {
-				content |= !(f & kFEmpty);
-				open |= !(f & kFOpaqueCube) || (lane < 2 && !(fe & kFOpaqueCube));
-			} else if (yin || zin) { // a face-adjacent layer row (x in [0, 32))
-				open |= !(f & kFOpaqueCube);
+			for (int j = 0; j < kBatch; ++j) {
+				const int row = row0 + j, y = row / kCls - 1, z = row % kCls - 1;
+				if (row >= kRows) // the same for the whole warp
+					break;
+				uint16_t *dst = S.cell + row * kCls;
+				dst[lane + 1] = (uint16_t)(c[j] << 8);
+				if (lane < 2)
+					dst[lane ? kCls - 1 : 0] = (uint16_t)(ce[j] << 8);
+				const uint8_t f = S.cflags[c[j]], fe = S.cflags[ce[j]];
+				const uint32_t oc = __ballot_sync(0xffffffffu, f & kFOpaqueCube);
+				const uint32_t em = __ballot_sync(0xffffffffu, f & kFEmpty);
+				const uint32_t oce = __ballot_sync(0xffffffffu, lane < 2 && (fe & kFOpaqueCube));
+				const uint32_t eme = __ballot_sync(0xffffffffu, lane < 2 && (fe & kFEmpty));
+				if (lane == 0) {
+					S.aux.pl.oc[row] = (uint64_t)(oce & 1u) | ((uint64_t)oc << 1) | ((uint64_t)((oce >> 1) & 1u) << 33);
+					S.aux.pl.em[row] = (uint64_t)(eme & 1u) | ((uint64_t)em << 1) | ((uint64_t)((eme >> 1) & 1u) << 33);
+				}
+				const bool yin = y >= 0 && y < kChunk, zin = z >= 0 && z < kChunk;
+				if (yin && zin) {
+					content |= !(f & kFEmpty);
+					open |= !(f & kFOpaqueCube) || (lane < 2 && !(fe & kFOpaqueCube));
+					custom |= (S.cmesh[c[j] >> 5] >> (c[j] & 31)) & 1u;
+				} else if (yin || zin) { // a face-adjacent layer row (x in [0, 32))
+					open |= !(f & kFOpaqueCube);
+				}
 			}
 		}
 	}
 	content = __syncthreads_or(content);
 	open = __syncthreads_or(open);
+	has_custom = __syncthreads_or(custom);
 	return !content || !open;
 }
 
@@ -835,13 +881,14 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 	if (tid < 4)
 		S.misc[kClaimComplex + tid] = 0; // the stage's barriers (and, in a cluster, the relight's) order
 	                                     // this before any CTA's plane phases
-	const bool blank = stage_classes(S, T);
+	bool has_custom;
+	const bool blank = stage_classes(S, T, has_custom);
 
 	uint32_t qo = 0, qt = 0;
 	uint32_t eo = 0, et = 0;
 	if (!blank) {
 		uint32_t co = 0, ct = 0, to, tt;
-		if (lead)
+		if (lead && has_custom) // no inner block with a custom mesh: nothing to count
 			custom_count(S, tid * kBlocksPerThread, co, ct);
 		block_scan2(S, co, ct, eo, et, to, tt);
 		if (S.lvl[26])
@@ -905,7 +952,7 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		return;
 
 	const Emit E{A.verts, A.idx, q0, qo};
-	if (lead)
+	if (lead && has_custom)
 		custom_emit(S, E, tid * kBlocksPerThread, eo, et, eo + et);
 	planes_emit(S, E, sp);
 	__syncthreads(); // every quad's box and closing position is in before the descriptors are written
