@@ -244,7 +244,9 @@ def ours(args):
     need_q, need_m, _ = plan.result(check=False)
     plan.close()
     arena = batch.Arena(int(need_q * 1.05) + 1024, int(need_m * 1.05) + 64, n, local)
-    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, batch.PERSISTENT)
+    # the autotuner times the persistent variants on this batch and keeps the fastest
+    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, batch.AUTO)
+    variant, variant_name, variant_ms = plan.variant()
 
     for _ in range(args.warmup):
         plan.launch(sp)
@@ -360,7 +362,8 @@ def ours(args):
             "vs_baseline": None, "dtype": "u16",
             "data": "synthetic: seeded worlds generated in-process (the reference publishes no benchmark data)",
             "config": {"workload": workload_name(args), "chunks_per_gpu": n, "form": "batched persistent "
-                       "work-stealing kernel, CUDA graph", "parallelism": f"replicas x{world}",
+                       "work-stealing kernel, CUDA graph", "autotuned_variant": variant_name,
+                       "variant_ms": dict(zip(batch.VARIANTS, variant_ms)), "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2: pool {w.n_chunks * 66560 / 1e6:.0f} MB, output "
                              f"{(44 * quads) / 1e6:.0f} MB per step"},
             "quads_per_s": quads_all / (ms_total / 1e3),
@@ -373,8 +376,8 @@ def ours(args):
                          "peak_source": f"{peak_kind} ({'MEASURED_PEAKS.json hbm_gbs' if peak_kind == 'measured' else 'fallback'})",
                          "algorithmic_bytes_per_launch": algo_bytes},
             "serving": serving,
-            # per step the plan's graph runs 17 kernels: planes, 15 light levels, mesh
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * 17,
+            # per step the plan's graph runs planes, 15 light levels (light-pass variant only) and the mesher
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * (17 if variant == 0 else 2),
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -14,7 +14,9 @@ import numpy as np
 
 from .mesher import HC_OK, HcError, MESH_DESC_DTYPE, BlockMesh, Context, library
 
-PERSISTENT, PER_CHUNK = 0, 1
+PERSISTENT, PER_CHUNK, AUTO = 0, 1, 2
+VARIANTS = ("light pass, one CTA per chunk", "window relight, one CTA per chunk", "window relight, 2-CTA clusters",
+            "window relight, 4-CTA clusters")
 RESULT_OK, RESULT_ARENA_FULL, RESULT_BAD_SLOT = 0, 1, 2
 
 
@@ -42,6 +44,7 @@ def _bind(lib):
     lib.hc_batch_plan_launch.argtypes = [vp, vp]
     lib.hc_batch_plan_result.argtypes = [vp, P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint32)]
     lib.hc_batch_plan_download.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint32, vp, vp, vp, vp]
+    lib.hc_batch_plan_variant.argtypes = [vp, P(ctypes.c_int), vp]
     lib._batch_bound = True
     return lib
 
@@ -139,6 +142,13 @@ class BatchPlan:
 
     def launch(self, stream=None):
         self.ctx.check(self.lib.hc_batch_plan_launch(self.handle, stream), "hc_batch_plan_launch")
+
+    def variant(self):
+        """(variant index, its description, ms per variant as timed by the autotuner)."""
+        v = ctypes.c_int()
+        ms = np.zeros(4, np.float32)
+        self.lib.hc_batch_plan_variant(self.handle, ctypes.byref(v), ms.ctypes.data)
+        return v.value, VARIANTS[v.value], [float(x) for x in ms]
 
     def result(self, check: bool = True):
         """(quads, meshes, failed chunks) of the last launch (waits for it)."""

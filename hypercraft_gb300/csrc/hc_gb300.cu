@@ -309,6 +309,9 @@ struct hc_batch_plan {
 	hc_batch_arena arena{};
 	int mode = HC_BATCH_PERSISTENT;
 	int grid = 0;
+	int variant = HC_VARIANT_LIGHT_PASS;
+	float variant_ms[4] = {0, 0, 0, 0};
+	int cluster_grid[4] = {0, 0, 0, 0}; // persistent grid of the cluster variants
 	int32_t *d_slots = nullptr;            // distinct valid slots the batch reads (their planes are refreshed)
 	uint32_t n_slots = 0;
 	// batch light pass (persistent form): the distinct slots are the batch's chunks 0..n_slots-1
@@ -807,6 +810,31 @@ Arena plan_arena(const hc_batch_plan *p) {
 	             p->arena.results};
 }
 
+cudaLaunchConfig_t cluster_config(dim3 grid, size_t smem, cudaStream_t st, cudaLaunchAttribute *attr, int csize) {
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = grid;
+	cfg.blockDim = dim3(kThreads);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = st;
+	attr[0].id = cudaLaunchAttributeClusterDimension;
+	attr[0].val.clusterDim.x = (unsigned)csize;
+	attr[0].val.clusterDim.y = 1;
+	attr[0].val.clusterDim.z = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	return cfg;
+}
+
+// CTAs of a persistent grid of the cluster kernel: as many clusters as fit at once.
+int cluster_grid_size(hc_ctx *ctx, int csize, int sms) {
+	cudaLaunchAttribute attr[1];
+	cudaLaunchConfig_t cfg = cluster_config(dim3(csize * ((sms + csize - 1) / csize)), ctx->smem_bytes, nullptr, attr, csize);
+	int clusters = 0;
+	if (cudaOccupancyMaxActiveClusters(&clusters, k_mesh_cluster, &cfg) != cudaSuccess || clusters < 1)
+		clusters = std::max(1, sms / csize);
+	return clusters * csize;
+}
+
 // Numbers the batch's distinct slots 0..n_slots-1 (their order in `slots`), rewrites the neighbour
 // table in those numbers and derives every batch chunk's face neighbours from the 3x3x3 blocks of
 // the table's rows (two slots are face neighbours when some row holds both, one step apart), then
@@ -866,7 +894,8 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		                                     p->pool->d_planes);
 		HC_CUDA(ctx, cudaGetLastError());
 	}
-	if (p->d_levels) {
+	const bool light_pass = p->variant == HC_VARIANT_LIGHT_PASS && p->d_levels;
+	if (light_pass) {
 		const LightPass L{p->d_slots, p->d_nb6, p->pool->d_planes, p->pool->d_blocks, p->d_levels, p->d_edges, p->n_slots};
 		for (int t = kLevels; t >= 1; --t) {
 			k_light_level<<<p->n_slots, kLightThreads, 0, st>>>(L, tables(ctx), t);
@@ -877,11 +906,20 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 	const Arena A = plan_arena(p);
 	unsigned int *work = reinterpret_cast<unsigned int *>(p->d_state + 2);
 	unsigned int *failed = reinterpret_cast<unsigned int *>(p->d_state + 3);
-	if (p->mode == HC_BATCH_PERSISTENT) {
-		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(p->pool->d_blocks, p->pool->d_heights, p->pool->d_planes,
-		                                                          p->pool->capacity, p->nbr, p->n, nullptr, work, failed,
-		                                                          tables(ctx), A, p->d_levels, p->d_edges,
-		                                                          p->d_nbr_local);
+	if (p->mode == HC_BATCH_PERSISTENT && p->variant >= HC_VARIANT_CLUSTER2) {
+		const int csize = p->variant == HC_VARIANT_CLUSTER2 ? 2 : 4;
+		cudaLaunchAttribute attr[1];
+		cudaLaunchConfig_t cfg = cluster_config(dim3(p->cluster_grid[p->variant]), ctx->smem_bytes, st, attr, csize);
+		HC_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_mesh_cluster, (const uint16_t *)p->pool->d_blocks,
+		                                (const int8_t *)p->pool->d_heights, (const uint32_t *)p->pool->d_planes,
+		                                p->pool->capacity, p->nbr, p->n, (const uint32_t *)nullptr, work, failed,
+		                                tables(ctx), A, (const uint32_t *)nullptr, (const uint32_t *)nullptr,
+		                                (const int32_t *)nullptr, csize));
+	} else if (p->mode == HC_BATCH_PERSISTENT) {
+		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(
+		    p->pool->d_blocks, p->pool->d_heights, p->pool->d_planes, p->pool->capacity, p->nbr, p->n, nullptr, work,
+		    failed, tables(ctx), A, light_pass ? p->d_levels : nullptr, light_pass ? p->d_edges : nullptr,
+		    light_pass ? p->d_nbr_local : nullptr);
 		HC_CUDA(ctx, cudaGetLastError());
 	} else {
 		for (uint32_t i = 0; i < p->n; ++i) {
@@ -900,8 +938,11 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 	if (!ctx || !pool || !neighbours || !arena || !out || n == 0 || !arena->vertices || !arena->indices ||
 	    !arena->meshes || !arena->results)
 		return HC_ERR_INVALID_ARG;
-	if (mode != HC_BATCH_PERSISTENT && mode != HC_BATCH_PER_CHUNK)
+	if (mode != HC_BATCH_PERSISTENT && mode != HC_BATCH_PER_CHUNK && mode != HC_BATCH_AUTO)
 		return fail(ctx, HC_ERR_INVALID_ARG, "unknown batch mode");
+	const bool autotune = mode == HC_BATCH_AUTO;
+	if (autotune)
+		mode = HC_BATCH_PERSISTENT;
 	if ((reinterpret_cast<uintptr_t>(arena->vertices) & 15u) || (reinterpret_cast<uintptr_t>(arena->indices) & 3u))
 		return fail(ctx, HC_ERR_INVALID_ARG, "vertices must be 16-byte and indices 4-byte aligned");
 	if (arena->quad_capacity > 0xffffffffull / 6)
@@ -923,6 +964,8 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 	if (ctas_per_sm > 0 && ctas_per_sm < per_sm)
 		per_sm = ctas_per_sm;
 	p->grid = sms * per_sm;
+	p->cluster_grid[HC_VARIANT_CLUSTER2] = cluster_grid_size(ctx, 2, sms);
+	p->cluster_grid[HC_VARIANT_CLUSTER4] = cluster_grid_size(ctx, 4, sms);
 	hc_status s = HC_OK;
 	// distinct valid slots named by the neighbour table
 	std::vector<int32_t> table((size_t)n * 27);
@@ -946,16 +989,63 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 		e = cudaMallocHost(&p->h_state, 4 * sizeof(unsigned long long));
 	if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT) {
 		e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
-		if (e == cudaSuccess)
+		// the variants to build: the light pass only, or (autotuning) all four, timed on this batch
+		const int first = HC_VARIANT_LIGHT_PASS, last = autotune ? HC_VARIANT_CLUSTER4 : HC_VARIANT_LIGHT_PASS;
+		float best_ms = 0.f;
+		for (int v = first; v <= last && e == cudaSuccess && s == HC_OK; ++v) {
+			p->variant = v;
+			cudaGraph_t graph = nullptr;
+			cudaGraphExec_t exec = nullptr;
 			e = cudaStreamBeginCapture(p->capture_stream, cudaStreamCaptureModeThreadLocal);
-		if (e == cudaSuccess) {
-			s = enqueue_plan(p, p->capture_stream);
-			cudaError_t e2 = cudaStreamEndCapture(p->capture_stream, &p->graph);
-			if (s == HC_OK)
-				e = e2;
+			if (e == cudaSuccess) {
+				s = enqueue_plan(p, p->capture_stream);
+				cudaError_t e2 = cudaStreamEndCapture(p->capture_stream, &graph);
+				if (s == HC_OK)
+					e = e2;
+			}
+			if (e == cudaSuccess && s == HC_OK)
+				e = cudaGraphInstantiate(&exec, graph, 0);
+			float ms = 0.f;
+			if (e == cudaSuccess && s == HC_OK && autotune) { // one warm run, then the mean of two
+				cudaEvent_t e0 = nullptr, e1 = nullptr;
+				e = cudaEventCreate(&e0);
+				if (e == cudaSuccess)
+					e = cudaEventCreate(&e1);
+				if (e == cudaSuccess)
+					e = cudaGraphLaunch(exec, p->capture_stream);
+				if (e == cudaSuccess)
+					e = cudaEventRecord(e0, p->capture_stream);
+				for (int r = 0; r < 2 && e == cudaSuccess; ++r)
+					e = cudaGraphLaunch(exec, p->capture_stream);
+				if (e == cudaSuccess)
+					e = cudaEventRecord(e1, p->capture_stream);
+				if (e == cudaSuccess)
+					e = cudaEventSynchronize(e1);
+				if (e == cudaSuccess)
+					e = cudaEventElapsedTime(&ms, e0, e1);
+				ms *= 0.5f;
+				p->variant_ms[v] = ms;
+				if (e0)
+					cudaEventDestroy(e0);
+				if (e1)
+					cudaEventDestroy(e1);
+			}
+			if (e == cudaSuccess && s == HC_OK && (!p->exec || ms < best_ms)) {
+				if (p->exec)
+					cudaGraphExecDestroy(p->exec), cudaGraphDestroy(p->graph);
+				p->exec = exec, p->graph = graph, best_ms = ms;
+				exec = nullptr, graph = nullptr;
+			}
+			if (exec)
+				cudaGraphExecDestroy(exec);
+			if (graph)
+				cudaGraphDestroy(graph);
 		}
-		if (e == cudaSuccess && s == HC_OK)
-			e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+		if (autotune && e == cudaSuccess && s == HC_OK) { // the variant whose graph was kept
+			for (int v = first; v <= last; ++v)
+				if (p->variant_ms[v] == best_ms)
+					p->variant = v;
+		}
 	}
 	if (e != cudaSuccess || s != HC_OK) {
 		if (s == HC_OK)
@@ -965,6 +1055,17 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 		return s;
 	}
 	*out = p;
+	return HC_OK;
+}
+
+hc_status hc_batch_plan_variant(const hc_batch_plan *plan, int *variant, float ms[4]) {
+	if (!plan)
+		return HC_ERR_INVALID_ARG;
+	if (variant)
+		*variant = plan->variant;
+	if (ms)
+		for (int v = 0; v < 4; ++v)
+			ms[v] = plan->variant_ms[v];
 	return HC_OK;
 }
 
@@ -1145,31 +1246,6 @@ hc_status world_enqueue_evict(hc_world *w, const int32_t *d_pos, uint32_t n, cud
 }
 
 Arena world_arena(const hc_world *w, const hc_batch_arena *arena);
-
-cudaLaunchConfig_t cluster_config(dim3 grid, size_t smem, cudaStream_t st, cudaLaunchAttribute *attr, int csize) {
-	cudaLaunchConfig_t cfg = {};
-	cfg.gridDim = grid;
-	cfg.blockDim = dim3(kThreads);
-	cfg.dynamicSmemBytes = smem;
-	cfg.stream = st;
-	attr[0].id = cudaLaunchAttributeClusterDimension;
-	attr[0].val.clusterDim.x = (unsigned)csize;
-	attr[0].val.clusterDim.y = 1;
-	attr[0].val.clusterDim.z = 1;
-	cfg.attrs = attr;
-	cfg.numAttrs = 1;
-	return cfg;
-}
-
-// CTAs of a persistent grid of the cluster kernel: as many clusters as fit at once.
-int cluster_grid_size(hc_ctx *ctx, int csize, int sms) {
-	cudaLaunchAttribute attr[1];
-	cudaLaunchConfig_t cfg = cluster_config(dim3(csize * ((sms + csize - 1) / csize)), ctx->smem_bytes, nullptr, attr, csize);
-	int clusters = 0;
-	if (cudaOccupancyMaxActiveClusters(&clusters, k_mesh_cluster, &cfg) != cudaSuccess || clusters < 1)
-		clusters = std::max(1, sms / csize);
-	return clusters * csize;
-}
 
 hc_status world_enqueue_remesh(hc_world *w, const hc_batch_arena *arena, cudaStream_t st) {
 	hc_ctx *ctx = w->ctx;

@@ -161,15 +161,28 @@ hc_status hc_mesh_infos(hc_ctx *ctx, const hc_mesh_desc *meshes, uint32_t n, con
 
 typedef struct hc_batch_plan hc_batch_plan;
 
-enum { HC_BATCH_PERSISTENT = 0, HC_BATCH_PER_CHUNK = 1 };
+enum { HC_BATCH_PERSISTENT = 0, HC_BATCH_PER_CHUNK = 1, HC_BATCH_AUTO = 2 };
+/* Persistent-form variants (see HC_BATCH_AUTO): */
+enum {
+	HC_VARIANT_LIGHT_PASS = 0, /* batch light pass, then one CTA per chunk */
+	HC_VARIANT_WINDOW = 1,     /* each chunk relights its own 62^3 window, one CTA per chunk */
+	HC_VARIANT_CLUSTER2 = 2,   /* window relight, two CTAs (a cluster) per chunk */
+	HC_VARIANT_CLUSTER4 = 3    /* window relight, four CTAs per chunk */
+};
 
 /* Plans meshing `n` chunks whose neighbour slot table (n x 27 int32, device) is `neighbours`:
- * mode HC_BATCH_PERSISTENT captures {cursor reset, persistent work-stealing kernel} as a CUDA
- * graph; HC_BATCH_PER_CHUNK launches the single-chunk kernel once per chunk. `ctas_per_sm`
- * (0 = automatic) sizes the persistent grid. */
+ * mode HC_BATCH_PERSISTENT captures {plane refresh, batch light pass, persistent work-stealing
+ * kernel} as a CUDA graph; HC_BATCH_PER_CHUNK launches the single-chunk kernel once per chunk;
+ * HC_BATCH_AUTO is an autotuner: it captures every HC_VARIANT_* of the persistent form, times each
+ * on this batch (its arena receives the output, identical for all) and keeps the fastest. Large
+ * batches favour the light pass; a few heavy chunks favour clusters. `ctas_per_sm` (0 = automatic)
+ * sizes the persistent grid. */
 hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighbours, uint32_t n,
                                const hc_batch_arena *arena, int mode, int ctas_per_sm, hc_batch_plan **out);
 void hc_batch_plan_destroy(hc_batch_plan *plan);
+/* The persistent variant the plan runs and, after HC_BATCH_AUTO, the time each variant took on
+ * the batch (ms; 0 where not timed). */
+hc_status hc_batch_plan_variant(const hc_batch_plan *plan, int *variant, float ms[4]);
 /* Enqueues one run of the plan on `stream` (NULL = the context stream). */
 hc_status hc_batch_plan_launch(hc_batch_plan *plan, void *stream);
 /* Waits for the last launch and reads the arena cursors: quads and meshes written (or required,

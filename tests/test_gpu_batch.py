@@ -12,8 +12,9 @@ def _small_world(kind):
 
 
 @pytest.mark.parametrize("kind", ["scale", "mixture"])
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_batch_matches_oracle(ctx, oracle, kind, mode):
+    """Persistent plan, per-chunk plan and the autotuned plan (whichever variant it keeps)."""
     from hypercraft_gb300 import batch
     w = _small_world(kind)
     rw = batch.upload_world(ctx, w)
