@@ -33,7 +33,7 @@ RESULT_BYTES = 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="scale", choices=["scale", "mixture", "edits", "serve"])
@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the per-chunk form (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--variant", default="auto", choices=["auto", "0", "1", "2", "3"],
+                    help="persistent variant: auto-tuned, or pinned (profiling runs: a profiler's per-launch cost "
+                         "distorts the autotuner's timing)")
     return ap.parse_args()
 
 
@@ -72,6 +75,16 @@ def workload_name(args):
             f"10% random fill / 5% checkerboard, shuffled, ring of lit air chunks")
 
 
+# DRAM bytes (read + write) of one k_mesh_batch launch on the default scale workload, from one
+# ncu capture (profiles/k_mesh_batch_scale32x8x32_dram.md gives the command); other workloads: null
+MESH_TRAFFIC_BYTES = {"scale:32x8x32": 2.065e9}
+
+
+def mesh_traffic(args):
+    nx, ny, nz = dims(args)
+    return MESH_TRAFFIC_BYTES.get(f"{args.workload}:{nx}x{ny}x{nz}")
+
+
 def hbm_peak():
     try:
         with open(PEAKS_FILE) as f:
@@ -93,10 +106,13 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.perf_counter()  # the sampler is running before the timed region starts
+            while not self.lines and time.perf_counter() - t0 < 2.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -193,7 +209,8 @@ def reference_arm(args):
     chunks = w.meshable()
     nbr = w.neighbour_table(chunks)
     threads = os.cpu_count()
-    sample = min(len(chunks), 2048)
+    # about 40k chunks of CPU work in all, whatever the step count (~10 s on 16 cores)
+    sample = min(len(chunks), 2048, max(128, 40960 // (args.warmup + args.steps)))
     rng = np.random.default_rng(1)
     times, quads = [], 0
     for step in range(args.warmup + args.steps):
@@ -204,6 +221,12 @@ def reference_arm(args):
             quads += q
     total = sum(times)
     value = sample * args.steps / total
+    # the reference client's own worker count (hardware_concurrency * 3 / 4, client/src/Application.cpp:248)
+    # and one runner's per-chunk latency, on bounded samples of the same chunks
+    ref_threads = max(1, threads * 3 // 4)
+    dt3, _, _ = cpu_run(w, chunks[pick], nbr[pick], runner, ref_threads)
+    one = min(sample, 128)
+    dt1, _, _ = cpu_run(w, chunks[pick[:one]], nbr[pick[:one]], runner, 1)
     line = {
         "impl": "reference", "metric": "chunks/s", "value": value, "unit": "chunks/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
@@ -211,7 +234,10 @@ def reference_arm(args):
         "config": {"workload": workload_name(args), "sample_chunks_per_step": sample},
         "quads_per_s": quads / total,
         "cpu_baseline": {"value": value, "unit": "chunks/s", "cores": threads, "kind": kind,
-                         "sample": f"{sample} random chunks of the workload per step, {threads} threads"},
+                         "sample": f"{sample} random chunks of the workload per step, {threads} threads",
+                         "reference_default_threads": ref_threads,
+                         "chunks_per_s_at_default_threads": sample / dt3,
+                         "single_thread_ms_per_chunk": 1e3 * dt1 / one},
         "e2e": {"value": value, "unit": "chunks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -245,7 +271,8 @@ def ours(args):
     plan.close()
     arena = batch.Arena(int(need_q * 1.05) + 1024, int(need_m * 1.05) + 64, n, local)
     # the autotuner times the persistent variants on this batch and keeps the fastest
-    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, batch.AUTO)
+    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena,
+                           batch.AUTO if args.variant == "auto" else batch.variant_mode(int(args.variant)))
     variant, variant_name, variant_ms = plan.variant()
 
     for _ in range(args.warmup):
@@ -272,9 +299,18 @@ def ours(args):
     value = chunks_all / (ms_total / 1e3)
     ms_step = ms_total / args.steps
 
+    # the dominant kernel alone: CUDA events recorded inside the plan's graph around its stages,
+    # read after each of K further launches
+    stages = np.zeros(3)
+    for _ in range(args.steps):
+        plan.launch(sp)
+        stages += plan.stage_ms()
+    stages /= args.steps
+    mesh_ms = float(stages[2])
+
     algo_bytes = n * (65536 + 1024 + RESULT_BYTES) + 44 * quads + DESC_BYTES * meshes
     peak, peak_kind = hbm_peak()
-    achieved = algo_bytes / (ms_step / 1e3) / 1e9
+    achieved = algo_bytes / (mesh_ms / 1e3) / 1e9
 
     # plain form: one kernel launch per chunk, same arena layout
     plain_value = None
@@ -372,8 +408,12 @@ def ours(args):
             "batched_vs_plain": (value / world / plain_value) if plain_value else None,
             "byte_exact_vs_plain_sample": plain_checked,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": mesh_traffic(args),
                          "peak_source": f"{peak_kind} ({'MEASURED_PEAKS.json hbm_gbs' if peak_kind == 'measured' else 'fallback'})",
+                         "kernel": "k_mesh_batch" if variant < 2 else "k_mesh_cluster",
+                         "kernel_ms": mesh_ms,
+                         "stage_ms": {"planes": float(stages[0]), "light_pass": float(stages[1]),
+                                      "mesh": float(stages[2])},
                          "algorithmic_bytes_per_launch": algo_bytes},
             "serving": serving,
             # per step the plan's graph runs planes, 15 light levels (light-pass variant only) and the mesher

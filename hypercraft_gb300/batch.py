@@ -15,6 +15,13 @@ import numpy as np
 from .mesher import HC_OK, HcError, MESH_DESC_DTYPE, BlockMesh, Context, library
 
 PERSISTENT, PER_CHUNK, AUTO = 0, 1, 2
+
+
+def variant_mode(v: int) -> int:
+    """Mode that builds persistent variant v alone (HC_BATCH_VARIANT)."""
+    return 16 + v
+
+
 VARIANTS = ("light pass, one CTA per chunk", "window relight, one CTA per chunk", "window relight, 2-CTA clusters",
             "window relight, 4-CTA clusters")
 RESULT_OK, RESULT_ARENA_FULL, RESULT_BAD_SLOT = 0, 1, 2
@@ -45,6 +52,7 @@ def _bind(lib):
     lib.hc_batch_plan_result.argtypes = [vp, P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint32)]
     lib.hc_batch_plan_download.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint32, vp, vp, vp, vp]
     lib.hc_batch_plan_variant.argtypes = [vp, P(ctypes.c_int), vp]
+    lib.hc_batch_plan_stage_ms.argtypes = [vp, vp]
     lib._batch_bound = True
     return lib
 
@@ -149,6 +157,12 @@ class BatchPlan:
         ms = np.zeros(4, np.float32)
         self.lib.hc_batch_plan_variant(self.handle, ctypes.byref(v), ms.ctypes.data)
         return v.value, VARIANTS[v.value], [float(x) for x in ms]
+
+    def stage_ms(self):
+        """Device time of the last launch's stages (waits for it): plane refresh, light pass, meshing."""
+        ms = np.zeros(3, np.float32)
+        self.ctx.check(self.lib.hc_batch_plan_stage_ms(self.handle, ms.ctypes.data), "hc_batch_plan_stage_ms")
+        return [float(x) for x in ms]
 
     def result(self, check: bool = True):
         """(quads, meshes, failed chunks) of the last launch (waits for it)."""

@@ -325,6 +325,9 @@ struct hc_batch_plan {
 	cudaGraphExec_t exec = nullptr;
 	cudaStream_t capture_stream = nullptr;
 	cudaStream_t last = nullptr;
+	// recorded around the stages of every run (event nodes of the graph): start, planes refreshed,
+	// light pass done, meshes done
+	cudaEvent_t stage_ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 struct hc_ctx {
@@ -884,8 +887,26 @@ cudaError_t plan_light_tables(hc_batch_plan *p, const std::vector<int32_t> &tabl
 	return e;
 }
 
+// In a stream capture an external record becomes an event-record node of the graph, so every
+// replay of the graph records the stage boundaries.
+// Outside a capture it is a plain record (the external flag is only valid while capturing).
+hc_status stage_mark(hc_batch_plan *p, int i, cudaStream_t st) {
+	if (!p->stage_ev[i])
+		return HC_OK;
+	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+	HC_CUDA(p->ctx, cudaStreamIsCapturing(st, &cs));
+	if (cs == cudaStreamCaptureStatusActive)
+		HC_CUDA(p->ctx, cudaEventRecordWithFlags(p->stage_ev[i], st, cudaEventRecordExternal));
+	else
+		HC_CUDA(p->ctx, cudaEventRecord(p->stage_ev[i], st));
+	return HC_OK;
+}
+
 hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 	hc_ctx *ctx = p->ctx;
+	hc_status s = stage_mark(p, 0, st);
+	if (s != HC_OK)
+		return s;
 	HC_CUDA(ctx, cudaMemsetAsync(p->d_state, 0, 4 * sizeof(unsigned long long), st));
 	if (p->n_slots) {
 		const uint64_t rows = (uint64_t)p->n_slots * kPlaneWords;
@@ -894,6 +915,8 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		                                     p->pool->d_planes);
 		HC_CUDA(ctx, cudaGetLastError());
 	}
+	if ((s = stage_mark(p, 1, st)) != HC_OK)
+		return s;
 	const bool light_pass = p->variant == HC_VARIANT_LIGHT_PASS && p->d_levels;
 	if (light_pass) {
 		const LightPass L{p->d_slots, p->d_nb6, p->pool->d_planes, p->pool->d_blocks, p->d_levels, p->d_edges, p->n_slots};
@@ -901,8 +924,9 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 			k_light_level<<<p->n_slots, kLightThreads, 0, st>>>(L, tables(ctx), t);
 			HC_CUDA(ctx, cudaGetLastError());
 		}
-
 	}
+	if ((s = stage_mark(p, 2, st)) != HC_OK)
+		return s;
 	const Arena A = plan_arena(p);
 	unsigned int *work = reinterpret_cast<unsigned int *>(p->d_state + 2);
 	unsigned int *failed = reinterpret_cast<unsigned int *>(p->d_state + 3);
@@ -928,7 +952,7 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		}
 		HC_CUDA(ctx, cudaGetLastError());
 	}
-	return HC_OK;
+	return stage_mark(p, 3, st);
 }
 
 } // namespace
@@ -938,10 +962,15 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 	if (!ctx || !pool || !neighbours || !arena || !out || n == 0 || !arena->vertices || !arena->indices ||
 	    !arena->meshes || !arena->results)
 		return HC_ERR_INVALID_ARG;
-	if (mode != HC_BATCH_PERSISTENT && mode != HC_BATCH_PER_CHUNK && mode != HC_BATCH_AUTO)
+	if (mode != HC_BATCH_PERSISTENT && mode != HC_BATCH_PER_CHUNK && mode != HC_BATCH_AUTO &&
+	    !(mode >= HC_BATCH_VARIANT(HC_VARIANT_LIGHT_PASS) && mode <= HC_BATCH_VARIANT(HC_VARIANT_CLUSTER4)))
 		return fail(ctx, HC_ERR_INVALID_ARG, "unknown batch mode");
 	const bool autotune = mode == HC_BATCH_AUTO;
-	if (autotune)
+	// the persistent variants to build: the light pass, one pinned variant, or (autotuning) all four
+	int first = HC_VARIANT_LIGHT_PASS, last = autotune ? HC_VARIANT_CLUSTER4 : HC_VARIANT_LIGHT_PASS;
+	if (mode >= HC_BATCH_VARIANT(0))
+		first = last = mode - HC_BATCH_VARIANT(0);
+	if (autotune || mode >= HC_BATCH_VARIANT(0))
 		mode = HC_BATCH_PERSISTENT;
 	if ((reinterpret_cast<uintptr_t>(arena->vertices) & 15u) || (reinterpret_cast<uintptr_t>(arena->indices) & 3u))
 		return fail(ctx, HC_ERR_INVALID_ARG, "vertices must be 16-byte and indices 4-byte aligned");
@@ -987,10 +1016,10 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 		e = cudaMalloc(&p->d_state, 4 * sizeof(unsigned long long));
 	if (e == cudaSuccess)
 		e = cudaMallocHost(&p->h_state, 4 * sizeof(unsigned long long));
+	for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+		e = cudaEventCreate(&p->stage_ev[i]);
 	if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT) {
 		e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
-		// the variants to build: the light pass only, or (autotuning) all four, timed on this batch
-		const int first = HC_VARIANT_LIGHT_PASS, last = autotune ? HC_VARIANT_CLUSTER4 : HC_VARIANT_LIGHT_PASS;
 		float best_ms = 0.f;
 		for (int v = first; v <= last && e == cudaSuccess && s == HC_OK; ++v) {
 			p->variant = v;
@@ -1058,6 +1087,17 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 	return HC_OK;
 }
 
+hc_status hc_batch_plan_stage_ms(hc_batch_plan *plan, float ms[3]) {
+	if (!plan || !ms)
+		return HC_ERR_INVALID_ARG;
+	hc_ctx *ctx = plan->ctx;
+	HC_CUDA(ctx, cudaSetDevice(ctx->device));
+	HC_CUDA(ctx, cudaEventSynchronize(plan->stage_ev[3]));
+	for (int i = 0; i < 3; ++i)
+		HC_CUDA(ctx, cudaEventElapsedTime(&ms[i], plan->stage_ev[i], plan->stage_ev[i + 1]));
+	return HC_OK;
+}
+
 hc_status hc_batch_plan_variant(const hc_batch_plan *plan, int *variant, float ms[4]) {
 	if (!plan)
 		return HC_ERR_INVALID_ARG;
@@ -1079,6 +1119,9 @@ void hc_batch_plan_destroy(hc_batch_plan *plan) {
 		cudaGraphDestroy(plan->graph);
 	if (plan->capture_stream)
 		cudaStreamDestroy(plan->capture_stream);
+	for (cudaEvent_t ev : plan->stage_ev)
+		if (ev)
+			cudaEventDestroy(ev);
 	cudaFree(plan->d_slots);
 	cudaFree(plan->d_nb6);
 	cudaFree(plan->d_nbr_local);

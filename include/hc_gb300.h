@@ -169,6 +169,9 @@ enum {
 	HC_VARIANT_CLUSTER2 = 2,   /* window relight, two CTAs (a cluster) per chunk */
 	HC_VARIANT_CLUSTER4 = 3    /* window relight, four CTAs per chunk */
 };
+/* Mode that builds exactly one persistent variant (no timing), e.g. to profile the one an
+ * HC_BATCH_AUTO plan chose: a profiler's per-launch cost distorts the autotuner's own timing. */
+#define HC_BATCH_VARIANT(v) (16 + (v))
 
 /* Plans meshing `n` chunks whose neighbour slot table (n x 27 int32, device) is `neighbours`:
  * mode HC_BATCH_PERSISTENT captures {plane refresh, batch light pass, persistent work-stealing
@@ -183,6 +186,10 @@ void hc_batch_plan_destroy(hc_batch_plan *plan);
 /* The persistent variant the plan runs and, after HC_BATCH_AUTO, the time each variant took on
  * the batch (ms; 0 where not timed). */
 hc_status hc_batch_plan_variant(const hc_batch_plan *plan, int *variant, float ms[4]);
+/* Waits for the last launch and gives the device time of its stages (ms, CUDA events recorded
+ * inside the plan): [0] bit-plane refresh, [1] batch light pass (0 for other variants), [2] the
+ * meshing kernel(s). No counterpart in the reference (its runner is not staged). */
+hc_status hc_batch_plan_stage_ms(hc_batch_plan *plan, float ms[3]);
 /* Enqueues one run of the plan on `stream` (NULL = the context stream). */
 hc_status hc_batch_plan_launch(hc_batch_plan *plan, void *stream);
 /* Waits for the last launch and reads the arena cursors: quads and meshes written (or required,

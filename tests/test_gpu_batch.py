@@ -12,15 +12,18 @@ def _small_world(kind):
 
 
 @pytest.mark.parametrize("kind", ["scale", "mixture"])
-@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("mode", [0, 1, 2, 17, 18, 19])
 def test_batch_matches_oracle(ctx, oracle, kind, mode):
-    """Persistent plan, per-chunk plan and the autotuned plan (whichever variant it keeps)."""
+    """Persistent plan, per-chunk plan, the autotuned plan (whichever variant it keeps) and each
+    other persistent variant pinned (window relight on one, two and four CTAs per chunk)."""
     from hypercraft_gb300 import batch
     w = _small_world(kind)
     rw = batch.upload_world(ctx, w)
     n = len(rw.chunks)
     arena = batch.Arena(3_000_000, 4096, n)
     plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, mode)
+    if mode >= 16:
+        assert plan.variant()[0] == mode - 16
     for _ in range(2):  # replay: cursors and work counter reset each launch
         plan.launch()
         q, m, f = plan.result()
