@@ -28,14 +28,24 @@ constexpr int kLtCells = kLt * kLt * kLt; // 39,304
 // The relight window [-15, 47)^3 as 62 x 62 rows of 62-bit words (bit = x + 15).
 constexpr int kWin = 62;
 constexpr int kWinRows = kWin * kWin; // 3,844
-// Per-chunk bit planes (pass, sun, level-15 emitters) as 32-bit rows (bit = x, row = z + 32 y),
-// plus one flag bit per row (the row holds an emitter of level 1..14), then the chunk's block
-// class ids, one byte per cell in the reference's cell order.
+// Per-chunk bit planes (pass, sun, level-15 emitters, opaque full cubes, blank blocks) as 32-bit
+// rows (bit = x, row = z + 32 y), plus one flag bit per row (the row holds an emitter of level
+// 1..14), a summary word per y layer (kLayer* bits: which kinds of block the layer and its edge
+// rows hold), then the chunk's block class ids, one byte per cell in the reference's cell order.
 constexpr int kPlaneWords = 1024;
-constexpr int kPlaneClassOff = 3 * kPlaneWords + 32;     // words
+enum { kPlanePass = 0, kPlaneSun = 1, kPlaneT15 = 2, kPlaneOpaque = 3, kPlaneEmpty = 4 };
+constexpr int kPlaneLowOff = 5 * kPlaneWords;             // words: per y layer the low-emitter row bits
+constexpr int kPlaneLayerOff = kPlaneLowOff + 32;         // words: per y layer a summary word
+constexpr int kPlaneClassOff = kPlaneLowOff + 64;         // words
 constexpr int kPlaneBits = kPlaneClassOff;                // the bit planes alone
-constexpr int kPlaneStride = kPlaneClassOff + 32768 / 4; // 45,184 bytes per chunk
-enum { kPlanePass = 0, kPlaneSun = 1, kPlaneT15 = 2 };
+constexpr int kPlaneStride = kPlaneClassOff + 32768 / 4; // 53,504 bytes per chunk
+// Layer summary bits: some block with a texture or custom mesh; some block that is not an opaque
+// full cube; the same for the x = 0 column, the x = 31 column, the z = 0 row and the z = 31 row;
+// some block with a custom mesh.
+enum : uint32_t {
+	kLayerContent = 1, kLayerOpen = 2, kLayerOpenX0 = 4, kLayerOpenX31 = 8, kLayerOpenZ0 = 16, kLayerOpenZ31 = 32,
+	kLayerCustom = 64
+};
 // Quad records staged for dense emission (two words each).
 constexpr int kQuadBuf = 4096;
 
@@ -238,19 +248,19 @@ __device__ __forceinline__ uint32_t div_small(uint32_t v, uint32_t n) { return n
 __host__ __device__ constexpr int cell_offset(int dx, int dy, int dz) { return dx + kCls * dz + kCls * kCls * dy; }
 #define HC_O(a, b, c) cell_offset(a, b, c)
 __constant__ int16_t c_front_off[6] = {HC_O(1, 0, 0), HC_O(-1, 0, 0), HC_O(0, 1, 0), HC_O(0, -1, 0), HC_O(0, 0, 1), HC_O(0, 0, -1)};
-__constant__ int16_t c_corner_off[6][4][3] = {
-    {{HC_O(1, 0, -1), HC_O(1, -1, -1), HC_O(1, -1, 0)}, {HC_O(1, 0, -1), HC_O(1, 1, -1), HC_O(1, 1, 0)},
-     {HC_O(1, 0, 1), HC_O(1, 1, 1), HC_O(1, 1, 0)}, {HC_O(1, 0, 1), HC_O(1, -1, 1), HC_O(1, -1, 0)}},
-    {{HC_O(-1, 0, -1), HC_O(-1, -1, -1), HC_O(-1, -1, 0)}, {HC_O(-1, 0, 1), HC_O(-1, -1, 1), HC_O(-1, -1, 0)},
-     {HC_O(-1, 0, 1), HC_O(-1, 1, 1), HC_O(-1, 1, 0)}, {HC_O(-1, 0, -1), HC_O(-1, 1, -1), HC_O(-1, 1, 0)}},
-    {{HC_O(0, 1, -1), HC_O(-1, 1, -1), HC_O(-1, 1, 0)}, {HC_O(0, 1, 1), HC_O(-1, 1, 1), HC_O(-1, 1, 0)},
-     {HC_O(0, 1, 1), HC_O(1, 1, 1), HC_O(1, 1, 0)}, {HC_O(0, 1, -1), HC_O(1, 1, -1), HC_O(1, 1, 0)}},
-    {{HC_O(0, -1, -1), HC_O(-1, -1, -1), HC_O(-1, -1, 0)}, {HC_O(0, -1, -1), HC_O(1, -1, -1), HC_O(1, -1, 0)},
-     {HC_O(0, -1, 1), HC_O(1, -1, 1), HC_O(1, -1, 0)}, {HC_O(0, -1, 1), HC_O(-1, -1, 1), HC_O(-1, -1, 0)}},
-    {{HC_O(0, -1, 1), HC_O(-1, -1, 1), HC_O(-1, 0, 1)}, {HC_O(0, -1, 1), HC_O(1, -1, 1), HC_O(1, 0, 1)},
-     {HC_O(0, 1, 1), HC_O(1, 1, 1), HC_O(1, 0, 1)}, {HC_O(0, 1, 1), HC_O(-1, 1, 1), HC_O(-1, 0, 1)}},
-    {{HC_O(0, -1, -1), HC_O(-1, -1, -1), HC_O(-1, 0, -1)}, {HC_O(0, 1, -1), HC_O(-1, 1, -1), HC_O(-1, 0, -1)},
-     {HC_O(0, 1, -1), HC_O(1, 1, -1), HC_O(1, 0, -1)}, {HC_O(0, -1, -1), HC_O(1, -1, -1), HC_O(1, 0, -1)}}};
+// The eight cells around the face-front cell in the face's plane, in the cyclic order in which
+// corner v of BlockMeshAlgo.hpp's light4_init (tables at 74-108) reads sides ring[2v] and
+// ring[2v + 2] (mod 8) and the corner ring[2v + 1]; each cell is loaded once per face.
+__constant__ int16_t c_ring_off[6][8] = {
+    {HC_O(1, -1, 0), HC_O(1, -1, -1), HC_O(1, 0, -1), HC_O(1, 1, -1), HC_O(1, 1, 0), HC_O(1, 1, 1), HC_O(1, 0, 1), HC_O(1, -1, 1)},
+    {HC_O(-1, 0, -1), HC_O(-1, -1, -1), HC_O(-1, -1, 0), HC_O(-1, -1, 1), HC_O(-1, 0, 1), HC_O(-1, 1, 1), HC_O(-1, 1, 0),
+     HC_O(-1, 1, -1)},
+    {HC_O(0, 1, -1), HC_O(-1, 1, -1), HC_O(-1, 1, 0), HC_O(-1, 1, 1), HC_O(0, 1, 1), HC_O(1, 1, 1), HC_O(1, 1, 0), HC_O(1, 1, -1)},
+    {HC_O(-1, -1, 0), HC_O(-1, -1, -1), HC_O(0, -1, -1), HC_O(1, -1, -1), HC_O(1, -1, 0), HC_O(1, -1, 1), HC_O(0, -1, 1),
+     HC_O(-1, -1, 1)},
+    {HC_O(-1, 0, 1), HC_O(-1, -1, 1), HC_O(0, -1, 1), HC_O(1, -1, 1), HC_O(1, 0, 1), HC_O(1, 1, 1), HC_O(0, 1, 1), HC_O(-1, 1, 1)},
+    {HC_O(0, -1, -1), HC_O(-1, -1, -1), HC_O(-1, 0, -1), HC_O(-1, 1, -1), HC_O(0, 1, -1), HC_O(1, 1, -1), HC_O(1, 0, -1),
+     HC_O(1, -1, -1)}};
 #undef HC_O
 
 __device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
@@ -258,14 +268,18 @@ __device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
 	const uint32_t cf = S.cell[base + c_front_off[face]];
 	const bool dp3 = id_direct(cf >> 8);
 	const uint32_t lf = cf & 0xffu;
+	uint32_t ring[8];
+#pragma unroll
+	for (int i = 0; i < 8; ++i)
+		ring[i] = S.cell[base + c_ring_off[face][i]];
 	Light4 r{0, 0, 0};
 #pragma unroll
 	for (int v = 0; v < 4; ++v) {
 		bool ip[3], dp[3];
 		uint32_t l[3];
 #pragma unroll
-		for (int b = 0; b < 3; ++b) {
-			const uint32_t c = S.cell[base + c_corner_off[face][v][b]];
+		for (int b = 0; b < 3; ++b) { // side, corner, side (the two sides play the same part)
+			const uint32_t c = ring[(2 * v + b) & 7];
 			ip[b] = id_indirect(c >> 8);
 			dp[b] = id_direct(c >> 8);
 			l[b] = c & 0xffu;

@@ -121,45 +121,66 @@ __device__ __forceinline__ void put_quad(Smem &S, const Emit &E, int st, uint32_
 
 // ------------------------------------------------------------------------------------- staging
 
-// Stages the block classes of [-1, 32]^3, one warp per (y, z) row with lanes over x (four rows in
-// flight), and builds the x-row bit planes of opaque full cubes and of blank blocks. Returns true
-// when the chunk can produce no quad: every inner block has no texture and no custom mesh, or every
-// inner block and every block of the six adjacent layers is an opaque full cube.
+// Stages the block classes of [-1, 32]^3, one warp per (y, z) row with lanes over x (twelve rows in
+// flight), and the x-row bit planes of opaque full cubes and of blank blocks (from the chunk planes
+// where there are planes, else built by ballots). Returns true when the chunk can produce no quad:
+// every inner block has no texture and no custom mesh, or every inner block and every block of the
+// six adjacent layers is an opaque full cube; has_custom: some inner block has a custom mesh.
 __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
-	// With the planes, the chunk's own 32 KB of class ids are copied into the plane-mask scratch
-	// (unused until the light and plane passes) by asynchronous 16-byte copies, all in flight at
-	// once; the apron's class ids come straight from the neighbours' planes.
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	constexpr int kRows = kCls * kCls, kBatch = 12; // 1156 rows; 12 in flight per warp
 	const uint8_t *own = reinterpret_cast<const uint8_t *>(&S.u);
 	if (S.pln[26]) {
+		// The blank test first, from the layer summaries of the chunk and its six face neighbours
+		// (one warp, 32 words each), so a blank chunk stages nothing.
+		__shared__ uint32_t s_blank, s_custom;
+		if (warp == 0) {
+			const uint32_t mine = __ldg(S.pln[26] + kPlaneLayerOff + lane);
+			const uint32_t xm = __ldg(S.pln[nb_index(-1, 0, 0)] + kPlaneLayerOff + lane);
+			const uint32_t xp = __ldg(S.pln[nb_index(kChunk, 0, 0)] + kPlaneLayerOff + lane);
+			const uint32_t zm = __ldg(S.pln[nb_index(0, 0, -1)] + kPlaneLayerOff + lane);
+			const uint32_t zp = __ldg(S.pln[nb_index(0, 0, kChunk)] + kPlaneLayerOff + lane);
+			const uint32_t ym = lane == 0 ? __ldg(S.pln[nb_index(0, -1, 0)] + kPlaneLayerOff + 31) : 0u;
+			const uint32_t yp = lane == 0 ? __ldg(S.pln[nb_index(0, kChunk, 0)] + kPlaneLayerOff + 0) : 0u;
+			const uint32_t open = (mine & kLayerOpen) | (xm & kLayerOpenX31) | (xp & kLayerOpenX0) |
+			                      (zm & kLayerOpenZ31) | (zp & kLayerOpenZ0) | ((ym | yp) & kLayerOpen);
+			const bool blank = !__any_sync(0xffffffffu, mine & kLayerContent) || !__any_sync(0xffffffffu, open);
+			const bool custom = __any_sync(0xffffffffu, mine & kLayerCustom);
+			if (lane == 0)
+				s_blank = blank, s_custom = custom;
+		}
+		__syncthreads();
+		has_custom = s_custom != 0;
+		if (s_blank)
+			return true;
+		// The chunk's own 32 KB of class ids are copied into the plane-mask scratch (unused until the
+		// light and plane passes) by asynchronous 16-byte copies, all in flight at once.
 		const char *src = reinterpret_cast<const char *>(S.pln[26] + kPlaneClassOff);
 		const uint32_t dst = (uint32_t)__cvta_generic_to_shared(own);
 		for (int i = threadIdx.x; i < 32768 / 16; i += kThreads)
 			asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16 * i), "l"(src + 16 * i) : "memory");
 		asm volatile("cp.async.commit_group;" ::: "memory");
-	}
-	for (int i = threadIdx.x; i < 256; i += kThreads) {
-		const DevClass k = T.classes[i];
-		S.classes[i] = k;
-		S.cflags[i] = k.flags;
-		// classes with a custom mesh, as a 256-bit set
-		const uint32_t cm = __ballot_sync(0xffffffffu, (k.mesh_meta & 3u) != 0);
-		if ((threadIdx.x & 31) == 0)
-			S.cmesh[i >> 5] = cm;
-	}
-	if (S.pln[26])
-		asm volatile("cp.async.wait_group 0;" ::: "memory");
-	__syncthreads();
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	constexpr int kRows = kCls * kCls, kBatch = 12; // 1156 rows; 12 in flight per warp
-	bool content = false, open = false, custom = false;
-	if (S.pln[26]) {
-		// class ids of the x = -1 and x = 32 cells of every row, gathered once (one thread each)
-		uint8_t *edge = reinterpret_cast<uint8_t *>(&S.u) + 32768; // [2][kRows], past the own ids
-		for (int i = threadIdx.x; i < 2 * kRows; i += kThreads) {
-			const int side = i / kRows, row = i - side * kRows, y = row / kCls - 1, z = row % kCls - 1;
-			edge[i] = class_byte(S, side ? kChunk : -1, y, z);
+		for (int i = threadIdx.x; i < 256; i += kThreads)
+			S.classes[i] = T.classes[i];
+		// Meanwhile, one thread per row of [-1, 32]^2: the opaque-cube and blank bits of the row from
+		// its chunk's planes with the x = -1 and x = 32 bits from the x neighbours' (bit x + 1), and
+		// the class ids of the row's two edge cells.
+		for (int row = threadIdx.x; row < kRows; row += kThreads) {
+			const int y = row / kCls - 1, z = row % kCls - 1, ry = ((y & 31) << 5) | (z & 31);
+			const uint32_t *P = S.pln[nb_index(0, y, z)], *Pm = S.pln[nb_index(-1, y, z)], *Pp = S.pln[nb_index(kChunk, y, z)];
+			const uint32_t oc = __ldg(P + kPlaneOpaque * kPlaneWords + ry), em = __ldg(P + kPlaneEmpty * kPlaneWords + ry);
+			const uint32_t ocm = __ldg(Pm + kPlaneOpaque * kPlaneWords + ry), emm = __ldg(Pm + kPlaneEmpty * kPlaneWords + ry);
+			const uint32_t ocp = __ldg(Pp + kPlaneOpaque * kPlaneWords + ry), emp = __ldg(Pp + kPlaneEmpty * kPlaneWords + ry);
+			const uint8_t e0 = class_byte(S, -1, y, z), e1 = class_byte(S, kChunk, y, z);
+			S.aux.pl.oc[row] = (uint64_t)(ocm >> 31) | ((uint64_t)oc << 1) | ((uint64_t)(ocp & 1u) << 33);
+			S.aux.pl.em[row] = (uint64_t)(emm >> 31) | ((uint64_t)em << 1) | ((uint64_t)(emp & 1u) << 33);
+			S.cell[row * kCls] = (uint16_t)(e0 << 8);
+			S.cell[row * kCls + kCls - 1] = (uint16_t)(e1 << 8);
 		}
+		asm volatile("cp.async.wait_group 0;" ::: "memory");
 		__syncthreads();
+		// class ids of the cells x in [0, 32) of every row: the chunk's own from the copy, the
+		// apron's from the neighbours' planes; one warp per row, lanes over x
 		for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
 			uint8_t c[kBatch];
 #pragma unroll
@@ -170,37 +191,26 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 			}
 #pragma unroll
 			for (int j = 0; j < kBatch; ++j) {
-				const int row = row0 + j, y = row / kCls - 1, z = row % kCls - 1;
-				if (row >= kRows) // the same for the whole warp
+				if (row0 + j >= kRows) // the same for the whole warp
 					break;
-				uint16_t *dst = S.cell + row * kCls;
-				dst[lane + 1] = (uint16_t)(c[j] << 8);
-				const uint8_t f = S.cflags[c[j]];
-				const uint32_t oc = __ballot_sync(0xffffffffu, f & kFOpaqueCube);
-				const uint32_t em = __ballot_sync(0xffffffffu, f & kFEmpty);
-				const bool yin = (unsigned)y < (unsigned)kChunk, zin = (unsigned)z < (unsigned)kChunk;
-				if (lane == 0) { // the two edge cells of the row
-					const uint8_t e0 = edge[row], e1 = edge[kRows + row];
-					dst[0] = (uint16_t)(e0 << 8);
-					dst[kCls - 1] = (uint16_t)(e1 << 8);
-					const uint8_t f0 = S.cflags[e0], f1 = S.cflags[e1];
-					S.aux.pl.oc[row] = (uint64_t)((f0 & kFOpaqueCube) != 0) | ((uint64_t)oc << 1) |
-					                   ((uint64_t)((f1 & kFOpaqueCube) != 0) << 33);
-					S.aux.pl.em[row] = (uint64_t)((f0 & kFEmpty) != 0) | ((uint64_t)em << 1) |
-					                   ((uint64_t)((f1 & kFEmpty) != 0) << 33);
-					if (yin && zin)
-						open |= !(f0 & kFOpaqueCube) || !(f1 & kFOpaqueCube);
-				}
-				if (yin && zin) {
-					content |= !(f & kFEmpty);
-					open |= !(f & kFOpaqueCube);
-					custom |= (S.cmesh[c[j] >> 5] >> (c[j] & 31)) & 1u;
-				} else if (yin || zin) { // a face-adjacent layer row (x in [0, 32))
-					open |= !(f & kFOpaqueCube);
-				}
+				S.cell[(row0 + j) * kCls + lane + 1] = (uint16_t)(c[j] << 8);
 			}
 		}
-	} else {
+		__syncthreads();
+		return false;
+	}
+	for (int i = threadIdx.x; i < 256; i += kThreads) {
+		const DevClass k = T.classes[i];
+		S.classes[i] = k;
+		S.cflags[i] = k.flags;
+		// classes with a custom mesh, as a 256-bit set
+		const uint32_t cm = __ballot_sync(0xffffffffu, (k.mesh_meta & 3u) != 0);
+		if ((threadIdx.x & 31) == 0)
+			S.cmesh[i >> 5] = cm;
+	}
+	__syncthreads();
+	bool content = false, open = false, custom = false;
+	{
 		for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
 			uint8_t c[kBatch], ce[kBatch];
 			uint16_t raw[kBatch], rawe[kBatch];
@@ -574,45 +584,63 @@ __device__ void plane_keys(Smem &S, const Split &sp) {
 	}
 }
 
+// 32 x 32 bit transpose across a warp: lane r holds row r (bit c = column c) on entry and column r
+// (bit c = row c) on return. Five butterfly rounds swap ever smaller off-diagonal blocks.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+	const int lane = threadIdx.x & 31;
+	uint32_t m = 0x0000ffffu;
+#pragma unroll
+	for (int j = 16; j != 0; j >>= 1, m ^= m << j) {
+		const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+		const bool upper = (lane & j) != 0;
+		const uint32_t t = (((upper ? y : x) >> j) ^ (upper ? x : y)) & m;
+		x ^= upper ? t : (t << j);
+	}
+	return x;
+}
+
 // Exact greedy scan of one plane from its masks (BlockMeshAlgo.hpp:345-477), one warp per plane.
-// Lane r holds row r's masks and consumed bits. For each row u (in order) the quads starting in
-// row u are its runs: maximal stretches of live cells whose right neighbours are equal (width
-// first); every run then grows down over whole rows while each of its cells equals the one above
-// (height), the runs of one row extending in lockstep and marking the cells they cover consumed.
+// For each row u (in order) the quads starting in row u are its runs: maximal stretches of live
+// (visible, not yet covered) cells whose right neighbours are equal (width first); every run then
+// grows down over whole rows while each of its cells equals the one above (height). A run's height
+// is therefore 1 + the least, over its columns, of the number of consecutive equal-below bits from
+// row u down: lane v holds column v of the equal-below mask (transposed once per plane) and of the
+// covered cells, and a segmented minimum over the run's lanes gives the height without walking the
+// rows. Cells below row u can only be covered by quads of row u itself (a quad from a row above
+// that reaches them also covers row u there), so runs never meet covered cells below.
 // on_row(u, starts, tmask, is_start, w, h) is called by the whole warp for every row with quads;
 // the quad of lane v (is_start) is (u, v, w, h) and its stream is bit v of tmask.
 template <typename F> __device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], F &&on_row) {
 	const int lane = threadIdx.x & 31;
-	const uint32_t rN = m[lane][0], rE = m[lane][1], rD = m[lane][2], rT = m[lane][3];
-	uint32_t consumed = 0; // of row `lane`
+	const uint32_t rN = m[lane][0], rE = m[lane][1], rT = m[lane][3];
+	const uint32_t Dc = warp_transpose32(m[lane][2]); // bit r: cell (r, lane) equals cell (r + 1, lane)
+	const uint32_t upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+	uint32_t Cc = 0;                                   // bit r: cell (r, lane) is covered
 	uint32_t rows = __ballot_sync(0xffffffffu, rN != 0);
 	while (rows) {
 		const int u = __ffs(rows) - 1;
 		rows &= rows - 1;
-		const uint32_t live = __shfl_sync(0xffffffffu, rN, u) & ~__shfl_sync(0xffffffffu, consumed, u);
+		const uint32_t live = __shfl_sync(0xffffffffu, rN, u) & ~__ballot_sync(0xffffffffu, (Cc >> u) & 1u);
 		if (!live)
 			continue;
 		const uint32_t Eu = __shfl_sync(0xffffffffu, rE, u), Tu = __shfl_sync(0xffffffffu, rT, u);
 		const uint32_t cont = live & (live << 1) & (Eu << 1); // bit v continues the run of v-1
 		const uint32_t starts = live & ~cont;
-		const bool is_start = (starts >> lane) & 1u;
+		const bool in_run = (live >> lane) & 1u, is_start = (starts >> lane) & 1u;
 		const uint32_t after = lane == 31 ? 0u : (cont >> (lane + 1));
-		const int w = __ffs(~after);
-		const uint32_t run = is_start ? (w == 32 ? 0xffffffffu : (((1u << w) - 1u) << lane)) : 0u;
-		int h = 1;
-		bool going = is_start;
-		for (int k = 1; u + k < 32; ++k) {
-			if (!__any_sync(0xffffffffu, going))
-				break;
-			const uint32_t below = __shfl_sync(0xffffffffu, rD, u + k - 1);
-			going = going && (below & run) == run;
-			const uint32_t grown = __reduce_or_sync(0xffffffffu, going ? run : 0u);
-			if (lane == u + k)
-				consumed |= grown;
-			if (going)
-				h = k + 1;
+		const int rem = __ffs(~after); // lanes from this one to the end of its run
+		// rows below u this column can grow over, then the minimum over the rest of the run
+		int dl = in_run ? __ffs(~(Dc >> u)) - 1 : 32;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const int o = __shfl_down_sync(0xffffffffu, dl, d);
+			if (d < rem)
+				dl = min(dl, o);
 		}
-		on_row(u, starts, Tu, is_start, w, h);
+		const int h = __shfl_sync(0xffffffffu, dl, 31 - __clz(starts & upto)) + 1; // the run's start
+		if (in_run)
+			Cc |= (h == 32 ? 0xffffffffu : ((1u << h) - 1u)) << u;
+		on_row(u, starts, Tu, is_start, rem, h);
 	}
 }
 

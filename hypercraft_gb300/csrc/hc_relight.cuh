@@ -87,7 +87,7 @@ __device__ void seed_from_planes(Smem &S, int r_lo, int r_hi) {
 #pragma unroll
 			for (int pl = 0; pl < 3; ++pl)
 				w[c][pl] = __ldg(P + pl * kPlaneWords + prow);
-			low |= __ldg(P + 3 * kPlaneWords + (prow >> 5)) >> (prow & 31);
+			low |= __ldg(P + kPlaneLowOff + (prow >> 5)) >> (prow & 31);
 		}
 		uint64_t v[3];
 #pragma unroll
@@ -280,11 +280,13 @@ __device__ void relight_window(Smem &S, const DevTables &T, const Split &sp = Sp
 // ------------------------------------------------------------------------------------ planes
 
 // Bit planes of one 32-cell row (y, z) of a chunk: pass (transparency != opaque), sunlit
-// (Chunk::GetSunlight) and emitters of level 15; returns whether the row holds an emitter of
-// level 1..14. Uniform rows (one raw value) take one lookup.
+// (Chunk::GetSunlight), emitters of level 15, opaque full cubes and blank blocks, the row's class
+// ids and its kLayer* summary bits (all but the z-row bits); returns whether the row holds an
+// emitter of level 1..14. Uniform rows (one raw value) take one lookup.
 __device__ __forceinline__ bool chunk_plane_row(const uint16_t *blk, const int8_t *hgt, const DevClass *classes,
                                                 const uint8_t *class_of, int y, int z, uint32_t &pass, uint32_t &sun,
-                                                uint32_t &t15, uint32_t cls[8]) {
+                                                uint32_t &t15, uint32_t cls[8], uint32_t &layer, uint32_t &oc,
+                                                uint32_t &em) {
 	const uint4 *row = reinterpret_cast<const uint4 *>(blk + (y * kChunk + z) * kChunk);
 	uint4 q[4];
 #pragma unroll
@@ -303,6 +305,11 @@ __device__ __forceinline__ bool chunk_plane_row(const uint16_t *blk, const int8_
 		pass = (k.flags & kFIndirect) ? 0xffffffffu : 0u;
 		t15 = k.light >= 15 ? 0xffffffffu : 0u;
 		low = k.light > 0 && k.light < 15;
+		layer = ((k.flags & kFEmpty) ? 0u : kLayerContent) |
+		        ((k.flags & kFOpaqueCube) ? 0u : (kLayerOpen | kLayerOpenX0 | kLayerOpenX31)) |
+		        ((k.mesh_meta & 3u) ? kLayerCustom : 0u);
+		oc = (k.flags & kFOpaqueCube) ? 0xffffffffu : 0u;
+		em = (k.flags & kFEmpty) ? 0xffffffffu : 0u;
 #pragma unroll
 		for (int i = 0; i < 8; ++i)
 			cls[i] = c * 0x01010101u;
@@ -310,6 +317,8 @@ __device__ __forceinline__ bool chunk_plane_row(const uint16_t *blk, const int8_
 #pragma unroll
 		for (int i = 0; i < 8; ++i)
 			cls[i] = 0;
+		uint32_t custom = 0;
+		oc = em = 0;
 #pragma unroll
 		for (int i = 0; i < 4; ++i) {
 			const uint32_t ws[4] = {q[i].x, q[i].y, q[i].z, q[i].w};
@@ -323,8 +332,13 @@ __device__ __forceinline__ bool chunk_plane_row(const uint16_t *blk, const int8_
 				t15 |= (uint32_t)(k.light >= 15) << x;
 				low |= k.light > 0 && k.light < 15;
 				cls[x >> 2] |= c << (8 * (x & 3));
+				em |= (uint32_t)((k.flags & kFEmpty) != 0) << x;
+				oc |= (uint32_t)((k.flags & kFOpaqueCube) != 0) << x;
+				custom |= k.mesh_meta & 3u;
 			}
 		}
+		layer = (~em ? kLayerContent : 0u) | (~oc ? kLayerOpen : 0u) | ((oc & 1u) ? 0u : kLayerOpenX0) |
+		        ((oc >> 31) ? 0u : kLayerOpenX31) | (custom ? kLayerCustom : 0u);
 	}
 	const uint4 *hr = reinterpret_cast<const uint4 *>(hgt + z * kChunk);
 	const uint4 h[2] = {__ldg(hr), __ldg(hr + 1)};
@@ -338,20 +352,30 @@ __device__ __forceinline__ bool chunk_plane_row(const uint16_t *blk, const int8_
 	return low;
 }
 
-// Bit planes of chunks: one thread per 32-cell row, 32 rows (one flag word) per warp.
+// Bit planes of chunks: one thread per 32-cell row, 32 rows (one flag word, one layer) per warp.
 __device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hgt, const DevClass *cls_smem,
                                            const uint8_t *class_of, int r, uint32_t *out) {
-	uint32_t pass, sun, t15, cls[8];
-	const bool low = chunk_plane_row(blk, hgt, cls_smem, class_of, r >> 5, r & 31, pass, sun, t15, cls);
+	uint32_t pass, sun, t15, cls[8], layer, oc, em;
+	const bool low = chunk_plane_row(blk, hgt, cls_smem, class_of, r >> 5, r & 31, pass, sun, t15, cls, layer, oc, em);
 	out[kPlanePass * kPlaneWords + r] = pass;
+	out[kPlaneOpaque * kPlaneWords + r] = oc;
+	out[kPlaneEmpty * kPlaneWords + r] = em;
 	out[kPlaneSun * kPlaneWords + r] = sun;
 	out[kPlaneT15 * kPlaneWords + r] = t15;
 	uint4 *co = reinterpret_cast<uint4 *>(out + kPlaneClassOff + 8 * r);
 	co[0] = make_uint4(cls[0], cls[1], cls[2], cls[3]);
 	co[1] = make_uint4(cls[4], cls[5], cls[6], cls[7]);
 	const uint32_t lows = __ballot_sync(0xffffffffu, low);
-	if ((threadIdx.x & 31) == 0)
-		out[3 * kPlaneWords + (r >> 5)] = lows;
+	// the warp's rows are the layer y = r / 32, lane = z
+	const uint32_t z = (uint32_t)(r & 31);
+	const uint32_t sum = __reduce_or_sync(0xffffffffu, layer & (kLayerContent | kLayerOpen | kLayerOpenX0 | kLayerOpenX31 |
+	                                                             kLayerCustom)) |
+	                     (__reduce_or_sync(0xffffffffu, z == 0 ? layer : 0u) & kLayerOpen ? kLayerOpenZ0 : 0u) |
+	                     (__reduce_or_sync(0xffffffffu, z == 31 ? layer : 0u) & kLayerOpen ? kLayerOpenZ31 : 0u);
+	if ((threadIdx.x & 31) == 0) {
+		out[kPlaneLowOff + (r >> 5)] = lows;
+		out[kPlaneLayerOff + (r >> 5)] = sum;
+	}
 }
 
 
@@ -460,7 +484,7 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 	for (int k = 0; k < kLightRows; ++k) {
 		const int r = tid + k * kLightThreads;
 		pass[k] = __ldg(P + kPlanePass * kPlaneWords + r);
-		lows[k] = __ldg(P + 3 * kPlaneWords + (r >> 5));
+		lows[k] = __ldg(P + kPlaneLowOff + (r >> 5));
 		if (t == kLevels) {
 			s[k][0] = __ldg(P + kPlaneSun * kPlaneWords + r);
 			s[k][1] = __ldg(P + kPlaneT15 * kPlaneWords + r);
@@ -508,6 +532,24 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 	}
 }
 
+// Light bytes of the eight cells x = 8g .. 8g + 7 from the eight digit planes of a row (sun digits
+// 0-3, then torch digits 0-3): byte g of every plane gathered into one 8 x 8 bit matrix (row k =
+// plane k), transposed so that byte j holds bit x = 8g + j of every plane, by the three-step 8 x 8
+// bit-matrix transpose of Warren, Hacker's Delight, section 7-3.
+__device__ __forceinline__ uint64_t light_bytes8(const uint32_t w[8], int g) {
+	const uint32_t sel = (uint32_t)g | ((uint32_t)(g + 4) << 4);
+	const uint32_t lo = __byte_perm(__byte_perm(w[0], w[1], sel), __byte_perm(w[2], w[3], sel), 0x5410);
+	const uint32_t hi = __byte_perm(__byte_perm(w[4], w[5], sel), __byte_perm(w[6], w[7], sel), 0x5410);
+	uint64_t x = ((uint64_t)hi << 32) | lo, t;
+	t = (x ^ (x >> 7)) & 0x00AA00AA00AA00AAull;
+	x ^= t ^ (t << 7);
+	t = (x ^ (x >> 14)) & 0x0000CCCC0000CCCCull;
+	x ^= t ^ (t << 14);
+	t = (x ^ (x >> 28)) & 0x00000000F0F0F0F0ull;
+	x ^= t ^ (t << 28);
+	return x;
+}
+
 // Light of [-1, 32]^3 from the batch light pass (instead of relight_window), decoded from the 15
 // nested level planes per channel into the low byte of every staged cell: a cell's light is the
 // number of levels that hold it, read as four binary digits by level_bits. Cells x in [0, 32) of
@@ -529,13 +571,13 @@ __device__ void light_from_levels(Smem &S) {
 			level_bits(lv, b[c]);
 		}
 		uint8_t *dst = light + 2 * (row * kLt + 1); // cell x = 0 of the row
-#pragma unroll 8
-		for (int x = 0; x < 32; ++x) {
-			uint32_t v = 0;
+		const uint32_t w[8] = {b[0][0], b[0][1], b[0][2], b[0][3], b[1][0], b[1][1], b[1][2], b[1][3]};
 #pragma unroll
-			for (int bit = 0; bit < 4; ++bit)
-				v |= ((b[0][bit] >> x) & 1u) << bit | ((b[1][bit] >> x) & 1u) << (bit + 4);
-			dst[2 * x] = (uint8_t)v;
+		for (int g = 0; g < 4; ++g) {
+			const uint64_t v = light_bytes8(w, g);
+#pragma unroll
+			for (int j = 0; j < 8; ++j)
+				dst[2 * (8 * g + j)] = (uint8_t)(v >> (8 * j));
 		}
 	}
 	for (int k = threadIdx.x; k < 2 * kLt * 3; k += kThreads) {
