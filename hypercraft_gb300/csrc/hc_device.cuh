@@ -46,8 +46,11 @@ enum : uint32_t {
 	kLayerContent = 1, kLayerOpen = 2, kLayerOpenX0 = 4, kLayerOpenX31 = 8, kLayerOpenZ0 = 16, kLayerOpenZ31 = 32,
 	kLayerCustom = 64
 };
-// Quad records staged for dense emission (two words each).
+// Quad records staged for dense emission (two words each): kQuadBuf in shared memory, then up to
+// kSpillRecs more per CTA in a global scratch (the most quads a chunk can have is 3 x 33 x 2 x 1,024
+// = 202,752; beyond the scratch the emission merges the planes again in windows).
 constexpr int kQuadBuf = 4096;
+constexpr uint32_t kSpillRecs = 1u << 17;
 
 // One block class: a distinct property row of the registry (65,536 raw values map onto < 256).
 struct DevClass {
@@ -145,6 +148,8 @@ struct Smem {
 	uint32_t aabb[2][kMaxMeshesPerStream][6];
 	uint32_t trig[2][kMaxMeshesPerStream];
 	uint32_t misc[16];
+	uint2 *spill;       // this CTA's quad records past kQuadBuf (global scratch), or null
+	uint32_t spill_cap; // records it holds
 	uint8_t plane_owner[kPlanes]; // cluster form, in CTA 0: the CTA that took each face plane
 	uint8_t mine[kPlanes];        // the face planes this CTA took, in the order it took them
 };

@@ -134,18 +134,29 @@ __device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
 	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// Prefetches what the next chunk of a batch reads first: its own class ids (or blocks) and the 27
-// chunks' bit planes.
+// Prefetches what the next chunk of a batch reads first. With the batch light pass the chunk reads
+// its own opaque/blank planes and layer words, its class ids and its light levels (the neighbours
+// only at the apron); with a window relight, the bit planes of all 27 chunks and its class ids;
+// without planes, its blocks.
 __device__ __forceinline__ void prefetch_item(const uint16_t *pool_blocks, const uint32_t *pool_planes, uint32_t pool_cap,
-                                              const int32_t *nbr, uint32_t item) {
+                                              const int32_t *nbr, uint32_t item, const uint32_t *levels,
+                                              const int32_t *nbr_local) {
 	const int t = threadIdx.x;
 	if (t < 27) {
 		const int32_t slot = nbr[(size_t)item * 27 + t];
 		if (slot >= 0 && (uint32_t)slot < pool_cap) {
-			if (pool_planes) {
-				prefetch_l2(pool_planes + (size_t)slot * kPlaneStride, kPlaneBits * sizeof(uint32_t));
+			const uint32_t *P = pool_planes + (size_t)slot * kPlaneStride;
+			if (pool_planes && levels) {
+				if (t == 26) {
+					prefetch_l2(P + kPlaneOpaque * kPlaneWords, (kPlaneClassOff - kPlaneOpaque * kPlaneWords) * sizeof(uint32_t));
+					prefetch_l2(P + kPlaneClassOff, 32768);
+					const size_t loc = (size_t)nbr_local[(size_t)item * 27 + 26];
+					prefetch_l2(levels + loc * kLevelSlotWords, (uint32_t)(kLevelSlotWords * sizeof(uint32_t)));
+				}
+			} else if (pool_planes) {
+				prefetch_l2(P, kPlaneBits * sizeof(uint32_t));
 				if (t == 26)
-					prefetch_l2(pool_planes + (size_t)slot * kPlaneStride + kPlaneClassOff, 32768);
+					prefetch_l2(P + kPlaneClassOff, 32768);
 			} else if (t == 26) {
 				for (int q = 0; q < 4; ++q)
 					prefetch_l2(pool_blocks + (size_t)slot * 32768 + q * 8192, 16384);
@@ -177,7 +188,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 		__syncthreads();
 		const uint32_t next = s_next;
 		if (next < n)
-			prefetch_item(pool_blocks, pool_planes, pool_cap, nbr, next);
+			prefetch_item(pool_blocks, pool_planes, pool_cap, nbr, next, levels, nbr_local);
 		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, levels, edges, nbr_local)) {
 			mesh_chunk_cta(S, T, A, item);
 			if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
@@ -321,6 +332,7 @@ struct hc_batch_plan {
 	uint32_t *d_edges = nullptr;    // per batch chunk: their x = 0 and x = 31 bits
 	unsigned long long *d_state = nullptr; // quad cursor, mesh cursor, work counter, failed chunks
 	unsigned long long *h_state = nullptr; // pinned
+	uint2 *d_spill = nullptr;              // quad records past the shared buffer, per CTA of any grid
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	cudaStream_t capture_stream = nullptr;
@@ -346,6 +358,7 @@ struct hc_ctx {
 	uint32_t *d_planes = nullptr;           // bit planes of the 27 chunks of a single-chunk call
 	unsigned long long *d_cursor = nullptr; // [0] quads, [1] meshes (as unsigned int in the low word)
 	uint32_t *d_results = nullptr;
+	uint2 *d_spill = nullptr; // quad records past the shared buffer, one CTA
 	uint32_t *h_results = nullptr; // pinned, 8 words
 	size_t smem_bytes = 0;
 	std::string err;
@@ -486,7 +499,7 @@ hc_status run_single(hc_ctx *ctx, const Refs27 &refs, uint2 *verts, uint16_t *id
                      unsigned long long quad_cap, unsigned int mesh_cap, cudaStream_t st) {
 	HC_CUDA(ctx, cudaMemsetAsync(ctx->d_cursor, 0, 2 * sizeof(unsigned long long), st));
 	Arena A{verts, idx, meshes, ctx->d_cursor, reinterpret_cast<unsigned int *>(ctx->d_cursor + 1), quad_cap, mesh_cap,
-	        ctx->d_results};
+	        ctx->d_results, ctx->d_spill};
 	Refs27 r = refs;
 	hc_status s = planes_for_refs(ctx, r, st);
 	if (s != HC_OK)
@@ -576,6 +589,7 @@ hc_status hc_ctx_create(int device, hc_ctx **out) {
 		chk(cudaMalloc(&ctx->d_planes, 27 * (size_t)kPlaneStride * sizeof(uint32_t)), "planes");
 		chk(cudaMalloc(&ctx->d_cursor, 2 * sizeof(unsigned long long)), "cursor");
 		chk(cudaMalloc(&ctx->d_results, 8 * sizeof(uint32_t)), "results");
+		chk(cudaMalloc(&ctx->d_spill, (size_t)kSpillRecs * sizeof(uint2)), "record scratch");
 		chk(cudaMallocHost(&ctx->h_results, 8 * sizeof(uint32_t)), "pinned results");
 	} while (0);
 	if (s != HC_OK) {
@@ -603,6 +617,7 @@ void hc_ctx_destroy(hc_ctx *ctx) {
 	cudaFree(ctx->d_planes);
 	cudaFree(ctx->d_cursor);
 	cudaFree(ctx->d_results);
+	cudaFree(ctx->d_spill);
 	cudaFreeHost(ctx->h_results);
 	if (ctx->stream)
 		cudaStreamDestroy(ctx->stream);
@@ -810,7 +825,8 @@ Arena plan_arena(const hc_batch_plan *p) {
 	             reinterpret_cast<unsigned int *>(p->d_state + 1),
 	             p->arena.quad_capacity,
 	             p->arena.mesh_capacity,
-	             p->arena.results};
+	             p->arena.results,
+	             p->d_spill};
 }
 
 cudaLaunchConfig_t cluster_config(dim3 grid, size_t smem, cudaStream_t st, cudaLaunchAttribute *attr, int csize) {
@@ -1016,6 +1032,13 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 		e = cudaMalloc(&p->d_state, 4 * sizeof(unsigned long long));
 	if (e == cudaSuccess)
 		e = cudaMallocHost(&p->h_state, 4 * sizeof(unsigned long long));
+	if (e == cudaSuccess) { // one record scratch per CTA of the largest grid the plan launches
+		const int ctas = mode == HC_BATCH_PER_CHUNK
+		                     ? 1
+		                     : std::max(p->grid, std::max(p->cluster_grid[HC_VARIANT_CLUSTER2],
+		                                                  p->cluster_grid[HC_VARIANT_CLUSTER4]));
+		e = cudaMalloc(&p->d_spill, (size_t)ctas * kSpillRecs * sizeof(uint2));
+	}
 	for (int i = 0; i < 4 && e == cudaSuccess; ++i)
 		e = cudaEventCreate(&p->stage_ev[i]);
 	if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT) {
@@ -1128,6 +1151,7 @@ void hc_batch_plan_destroy(hc_batch_plan *plan) {
 	cudaFree(plan->d_levels);
 	cudaFree(plan->d_edges);
 	cudaFree(plan->d_state);
+	cudaFree(plan->d_spill);
 	cudaFreeHost(plan->h_state);
 	delete plan;
 }
@@ -1214,6 +1238,7 @@ struct hc_world {
 	int sms = 0;
 	int cluster = 4;       // CTAs meshing one chunk (1: the one-CTA kernel)
 	int cluster_grid = 0;  // CTAs of the cluster kernel's persistent grid
+	uint2 *d_spill = nullptr; // quad records past the shared buffer, per CTA (at most one per SM)
 };
 
 namespace hc {
@@ -1339,7 +1364,8 @@ Arena world_arena(const hc_world *w, const hc_batch_arena *arena) {
 	             reinterpret_cast<unsigned int *>(w->d_state + 1),
 	             arena->quad_capacity,
 	             arena->mesh_capacity,
-	             arena->results};
+	             arena->results,
+	             w->d_spill};
 }
 
 hc_status check_arena(hc_ctx *ctx, const hc_batch_arena *arena, uint32_t cells) {
@@ -1458,6 +1484,7 @@ hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc,
 			e = cudaMemset(*p, 0, bytes > 0 ? bytes : 1);
 	};
 	A((void **)&w->d_slots, cells * sizeof(int32_t));
+	A((void **)&w->d_spill, (size_t)w->sms * kSpillRecs * sizeof(uint2));
 	A((void **)&w->d_flags, cells * sizeof(uint32_t));
 	A((void **)&w->d_flood, (size_t)w->flood_words * sizeof(uint32_t));
 	A((void **)&w->d_stale, (size_t)pool->capacity * sizeof(uint32_t));
@@ -1503,7 +1530,7 @@ void hc_world_destroy(hc_world *w) {
 	for (void *p : {(void *)w->d_slots, (void *)w->d_flags, (void *)w->d_flood, (void *)w->d_stale, (void *)w->d_counts,
 	                (void *)w->d_dirty_list, (void *)w->d_flood_list, (void *)w->d_hchg_list, (void *)w->d_stale_list,
 	                (void *)w->d_list, (void *)w->d_nbr, (void *)w->d_edits, (void *)w->d_sorted, (void *)w->d_nsorted,
-	                (void *)w->d_stage, (void *)w->d_state})
+	                (void *)w->d_stage, (void *)w->d_state, (void *)w->d_spill})
 		cudaFree(p);
 	cudaFreeHost(w->h_counts);
 	cudaFreeHost(w->h_state);

@@ -34,7 +34,7 @@ __device__ __forceinline__ int claim(uint32_t *counter) {
 		j = (int)atomicAdd(counter, 1u);
 	return __shfl_sync(0xffffffffu, j, 0);
 }
-enum : int { kClaimComplex = 12, kClaimKeys = 13, kClaimCount = 14, kMine = 15 }; // S.misc counters
+enum : int { kClaimComplex = 12, kClaimKeys = 13, kMine = 15 }; // S.misc counters
 
 // Next face plane for the calling warp's key pass. In a cluster the planes are taken from one
 // counter in CTA 0, so a heavy plane does not hold up a CTA with a fixed share; the taker records
@@ -506,7 +506,10 @@ __device__ __forceinline__ Key face_key(const Smem &S, int a, int s, int inv, in
 	return Key{(uint32_t)t | (l.ao << 16), l.sun, l.torch};
 }
 
-// Pass 2 (after the relight): equal-to-right and equal-to-below masks of every plane. The visible
+__device__ void plane_count_one(Smem &S, int p);
+
+// Pass 2 (after the relight): equal-to-right and equal-to-below masks of every plane, each plane
+// then merged and counted by the warp that built its masks (no block barrier in between). The visible
 // faces of a plane are taken in batches of whole rows (at most 32 faces), one face per lane, so
 // the light keys are computed by full warps; a face's right neighbour is the next lane and its
 // upper neighbour sits in this batch or in the previous one.
@@ -581,6 +584,7 @@ __device__ void plane_keys(Smem &S, const Split &sp) {
 			ub = ue;
 		}
 		__syncwarp();
+		plane_count_one(S, p);
 	}
 }
 
@@ -652,39 +656,38 @@ __device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, 
 	                  li | (lk << 16));
 }
 
-// Counts the quads of every plane (warp per plane) and keeps their records in shared memory while
+// Counts the quads of plane p (the calling warp) and keeps their records in shared memory while
 // they fit; misc[4] = records kept, misc[5] = 1 if some did not fit.
-__device__ void planes_count(Smem &S, const Split &sp) {
+__device__ void plane_count_one(Smem &S, int p) {
 	const int lane = threadIdx.x & 31;
 	const uint32_t lt = (1u << lane) - 1u;
-	const int n_mine = (int)S.misc[kMine];
-	for (int j = claim(&S.misc[kClaimCount]); j < n_mine; j = claim(&S.misc[kClaimCount])) {
-		const int p = S.mine[j];
-		uint32_t n_all = 0, n_st[2] = {0, 0};
-		warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
-			const uint32_t cnt = __popc(starts);
-			uint32_t base = 0;
-			if (lane == 0)
-				base = atomicAdd(&S.misc[4], cnt);
-			base = __shfl_sync(0xffffffffu, base, 0);
-			if (is_start) {
-				const int st = (int)((tmask >> lane) & 1u);
-				const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
-				const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
-				const uint32_t slot = base + __popc(starts & lt);
-				if (slot < (uint32_t)kQuadBuf)
-					S.aux.quads[slot] = quad_record(p, u, lane, w, h, st, li, lk);
-				else
-					S.misc[5] = 1;
-			}
-			n_all += cnt;
-			n_st[1] += __popc(starts & tmask);
-			n_st[0] += __popc(starts & ~tmask);
-		});
-		if (lane == 0) {
-			S.seg_cnt[0][1 + p] = n_st[0];
-			S.seg_cnt[1][1 + p] = n_st[1];
+	uint32_t n_all = 0, n_st[2] = {0, 0};
+	warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
+		const uint32_t cnt = __popc(starts);
+		uint32_t base = 0;
+		if (lane == 0)
+			base = atomicAdd(&S.misc[4], cnt);
+		base = __shfl_sync(0xffffffffu, base, 0);
+		if (is_start) {
+			const int st = (int)((tmask >> lane) & 1u);
+			const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
+			const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
+			const uint32_t slot = base + __popc(starts & lt);
+			const uint2 rec = quad_record(p, u, lane, w, h, st, li, lk);
+			if (slot < (uint32_t)kQuadBuf)
+				S.aux.quads[slot] = rec;
+			else if (slot - (uint32_t)kQuadBuf < S.spill_cap)
+				S.spill[slot - kQuadBuf] = rec;
+			else
+				S.misc[5] = 1;
 		}
+		n_all += cnt;
+		n_st[1] += __popc(starts & tmask);
+		n_st[0] += __popc(starts & ~tmask);
+	});
+	if (lane == 0) {
+		S.seg_cnt[0][1 + p] = n_st[0];
+		S.seg_cnt[1][1 + p] = n_st[1];
 	}
 }
 
@@ -729,7 +732,7 @@ __device__ __forceinline__ void emit_record(Smem &S, const Emit &E, bool valid, 
 	                valid ? S.seg_base[2][1 + p] + li : 0u);
 }
 
-// Emits the plane quads this CTA owns. Normally planes_count kept all their records; otherwise
+// Emits the plane quads this CTA owns. Normally plane_count_one kept all their records; otherwise
 // this CTA's quads are taken in windows of kQuadBuf (its planes in the order it took them, each
 // plane's quads in order), the planes overlapping a window merge again to stage that window's
 // records, and the whole CTA writes them. Emission of a window is spread over every thread: a
@@ -740,7 +743,8 @@ __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 		const uint32_t n = S.misc[4];
 		for (uint32_t j0 = (uint32_t)warp * 32; j0 < n; j0 += kThreads) {
 			const uint32_t j = j0 + lane;
-			emit_record(S, E, j < n, j < n ? S.aux.quads[j] : make_uint2(0, 0));
+			const uint2 r = j < n ? (j < (uint32_t)kQuadBuf ? S.aux.quads[j] : S.spill[j - kQuadBuf]) : make_uint2(0, 0);
+			emit_record(S, E, j < n, r);
 		}
 		return;
 	}
@@ -884,7 +888,8 @@ struct Arena {
 	unsigned int *mesh_cursor;
 	unsigned long long quad_cap;
 	unsigned int mesh_cap;
-	uint32_t *results; // per batch position: opaque quads, transparent quads, first mesh, mesh count, status
+	uint32_t *results;     // per batch position: opaque quads, transparent quads, first mesh, mesh count, status
+	uint2 *spill = nullptr; // kSpillRecs quad records per CTA of the grid (blockIdx.x), or null
 };
 
 enum : uint32_t { kChunkOk = 0, kChunkCapacity = 1 };
@@ -906,9 +911,13 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 	}
 	for (int i = tid; i < 2 * (kSegments + 1); i += kThreads)
 		S.seg_cnt[i / (kSegments + 1)][i % (kSegments + 1)] = 0;
-	if (tid < 4)
-		S.misc[kClaimComplex + tid] = 0; // the stage's barriers (and, in a cluster, the relight's) order
-	                                     // this before any CTA's plane phases
+	if (tid < 6) // claim counters, records kept, records overflow; the stage's barriers (and, in a
+	             // cluster, the relight's) order this before any CTA's plane phases
+		S.misc[tid < 4 ? kClaimComplex + tid : tid] = 0;
+	if (tid == 0) {
+		S.spill = A.spill ? A.spill + (size_t)blockIdx.x * kSpillRecs : nullptr;
+		S.spill_cap = A.spill ? kSpillRecs : 0u;
+	}
 	bool has_custom;
 	const bool blank = stage_classes(S, T, has_custom);
 
@@ -928,15 +937,11 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		__syncthreads();
 		if (sp.c > 1) // CTA 0's plane counter was reset for this chunk before any CTA takes from it
 			cooperative_groups::this_cluster().sync();
-		plane_keys(S, sp);
+		plane_keys(S, sp); // with each plane's quad count and records
 		if (tid == 0) {
 			S.seg_cnt[0][0] = to;
 			S.seg_cnt[1][0] = tt;
-			S.misc[4] = 0;
-			S.misc[5] = 0;
 		}
-		__syncthreads();
-		planes_count(S, sp);
 		__syncthreads();
 		if (sp.c > 1) { // every CTA takes the counts of the segments the others own
 			cg::cluster_group cl = cg::this_cluster();
