@@ -152,6 +152,7 @@ struct Smem {
 	uint32_t spill_cap; // records it holds
 	uint8_t plane_owner[kPlanes]; // cluster form, in CTA 0: the CTA that took each face plane
 	uint8_t mine[kPlanes];        // the face planes this CTA took, in the order it took them
+	uint8_t order[kPlanes];       // the face planes by falling face count: the order they are taken in
 };
 
 __device__ __forceinline__ int cls_index(int x, int y, int z) { return ((y + 1) * kCls + (z + 1)) * kCls + (x + 1); }

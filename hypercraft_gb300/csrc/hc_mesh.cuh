@@ -36,6 +36,32 @@ __device__ __forceinline__ int claim(uint32_t *counter) {
 }
 enum : int { kClaimComplex = 12, kClaimKeys = 13, kMine = 15 }; // S.misc counters
 
+// Orders the face planes by falling weight (visible faces and complex candidates, a tie to the
+// lower plane) into S.order, so that the key pass takes the heaviest planes first and its last
+// planes are light ones (longest-first scheduling). Weights sit in seg_base, unused until the scan.
+// Every CTA of a cluster computes the same order from the same masks.
+__device__ void order_planes(Smem &S) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	uint32_t *weight = &S.seg_base[0][0];
+	for (int p = warp; p < kPlanes; p += kWarps) {
+		const uint32_t w = __reduce_add_sync(0xffffffffu, __popc(S.u.masks[p][lane][0] | S.u.masks[p][lane][1]));
+		if (lane == 0)
+			weight[p] = w;
+	}
+	__syncthreads();
+	if (threadIdx.x < kPlanes) {
+		const int p = threadIdx.x;
+		const uint32_t w = weight[p];
+		int rank = 0;
+		for (int q = 0; q < kPlanes; ++q) {
+			const uint32_t wq = weight[q];
+			rank += (wq > w) || (wq == w && q < p);
+		}
+		S.order[rank] = (uint8_t)p;
+	}
+	__syncthreads();
+}
+
 // Next face plane for the calling warp's key pass. In a cluster the planes are taken from one
 // counter in CTA 0, so a heavy plane does not hold up a CTA with a fixed share; the taker records
 // the plane as its own (count and emission run where its masks are) and in CTA 0's owner table.
@@ -45,10 +71,14 @@ __device__ __forceinline__ int claim_plane(Smem &S, const Split &sp) {
 		if (sp.c > 1) {
 			cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
 			p = (int)atomicAdd(cl.map_shared_rank(&S.misc[kClaimKeys], 0), 1u);
-			if (p < kPlanes)
+			if (p < kPlanes) {
+				p = S.order[p];
 				cl.map_shared_rank(&S.plane_owner[0], 0)[p] = (uint8_t)sp.rank;
+			}
 		} else {
 			p = (int)atomicAdd(&S.misc[kClaimKeys], 1u);
+			if (p < kPlanes)
+				p = S.order[p];
 		}
 		if (p < kPlanes)
 			S.mine[atomicAdd(&S.misc[kMine], 1u)] = (uint8_t)p;
@@ -656,8 +686,21 @@ __device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, 
 	                  li | (lk << 16));
 }
 
-// Counts the quads of plane p (the calling warp) and keeps their records in shared memory while
-// they fit; misc[4] = records kept, misc[5] = 1 if some did not fit.
+// Record slot j: the first kQuadBuf in shared memory, then the CTA's global scratch; past both the
+// records are dropped and misc[5] says so (the emission then merges again in windows).
+__device__ __forceinline__ void put_record(Smem &S, uint32_t j, uint2 r) {
+	if (j < (uint32_t)kQuadBuf)
+		S.aux.quads[j] = r;
+	else if (j - (uint32_t)kQuadBuf < S.spill_cap)
+		S.spill[j - kQuadBuf] = r;
+	else
+		S.misc[5] = 1;
+}
+__device__ __forceinline__ uint2 get_record(const Smem &S, uint32_t j) {
+	return j < (uint32_t)kQuadBuf ? S.aux.quads[j] : S.spill[j - kQuadBuf];
+}
+
+// Counts the quads of plane p (the calling warp) and keeps their records; misc[4] = records kept.
 __device__ void plane_count_one(Smem &S, int p) {
 	const int lane = threadIdx.x & 31;
 	const uint32_t lt = (1u << lane) - 1u;
@@ -672,14 +715,7 @@ __device__ void plane_count_one(Smem &S, int p) {
 			const int st = (int)((tmask >> lane) & 1u);
 			const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
 			const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
-			const uint32_t slot = base + __popc(starts & lt);
-			const uint2 rec = quad_record(p, u, lane, w, h, st, li, lk);
-			if (slot < (uint32_t)kQuadBuf)
-				S.aux.quads[slot] = rec;
-			else if (slot - (uint32_t)kQuadBuf < S.spill_cap)
-				S.spill[slot - kQuadBuf] = rec;
-			else
-				S.misc[5] = 1;
+			put_record(S, base + __popc(starts & lt), quad_record(p, u, lane, w, h, st, li, lk));
 		}
 		n_all += cnt;
 		n_st[1] += __popc(starts & tmask);
@@ -743,8 +779,7 @@ __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 		const uint32_t n = S.misc[4];
 		for (uint32_t j0 = (uint32_t)warp * 32; j0 < n; j0 += kThreads) {
 			const uint32_t j = j0 + lane;
-			const uint2 r = j < n ? (j < (uint32_t)kQuadBuf ? S.aux.quads[j] : S.spill[j - kQuadBuf]) : make_uint2(0, 0);
-			emit_record(S, E, j < n, r);
+			emit_record(S, E, j < n, j < n ? get_record(S, j) : make_uint2(0, 0));
 		}
 		return;
 	}
@@ -935,6 +970,7 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		__syncthreads();
 		plane_visibility(S);
 		__syncthreads();
+		order_planes(S);
 		if (sp.c > 1) // CTA 0's plane counter was reset for this chunk before any CTA takes from it
 			cooperative_groups::this_cluster().sync();
 		plane_keys(S, sp); // with each plane's quad count and records
