@@ -642,9 +642,12 @@ __device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
 // covered cells, and a segmented minimum over the run's lanes gives the height without walking the
 // rows. Cells below row u can only be covered by quads of row u itself (a quad from a row above
 // that reaches them also covers row u there), so runs never meet covered cells below.
-// on_row(u, starts, tmask, is_start, w, h) is called by the whole warp for every row with quads;
-// the quad of lane v (is_start) is (u, v, w, h) and its stream is bit v of tmask.
-template <typename F> __device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], F &&on_row) {
+// For every row with quads the whole warp calls t = on_starts(starts) as soon as the row's quad
+// starts are known (so that what it starts, e.g. an atomic, overlaps the height search) and then
+// on_row(t, u, starts, tmask, is_start, w, h); the quad of lane v (is_start) is (u, v, w, h) and its
+// stream is bit v of tmask.
+template <typename G, typename F>
+__device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], G &&on_starts, F &&on_row) {
 	const int lane = threadIdx.x & 31;
 	const uint32_t rN = m[lane][0], rE = m[lane][1], rT = m[lane][3];
 	const uint32_t Dc = warp_transpose32(m[lane][2]); // bit r: cell (r, lane) equals cell (r + 1, lane)
@@ -660,6 +663,7 @@ template <typename F> __device__ __forceinline__ void warp_merge_plane(const uin
 		const uint32_t Eu = __shfl_sync(0xffffffffu, rE, u), Tu = __shfl_sync(0xffffffffu, rT, u);
 		const uint32_t cont = live & (live << 1) & (Eu << 1); // bit v continues the run of v-1
 		const uint32_t starts = live & ~cont;
+		const uint32_t token = on_starts(starts);
 		const bool in_run = (live >> lane) & 1u, is_start = (starts >> lane) & 1u;
 		const uint32_t after = lane == 31 ? 0u : (cont >> (lane + 1));
 		const int rem = __ffs(~after); // lanes from this one to the end of its run
@@ -674,7 +678,7 @@ template <typename F> __device__ __forceinline__ void warp_merge_plane(const uin
 		const int h = __shfl_sync(0xffffffffu, dl, 31 - __clz(starts & upto)) + 1; // the run's start
 		if (in_run)
 			Cc |= (h == 32 ? 0xffffffffu : ((1u << h) - 1u)) << u;
-		on_row(u, starts, Tu, is_start, rem, h);
+		on_row(token, u, starts, Tu, is_start, rem, h);
 	}
 }
 
@@ -705,12 +709,15 @@ __device__ void plane_count_one(Smem &S, int p) {
 	const int lane = threadIdx.x & 31;
 	const uint32_t lt = (1u << lane) - 1u;
 	uint32_t n_all = 0, n_st[2] = {0, 0};
-	warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
-		const uint32_t cnt = __popc(starts);
-		uint32_t base = 0;
+	const auto reserve = [&](uint32_t starts) {
+		uint32_t b = 0;
 		if (lane == 0)
-			base = atomicAdd(&S.misc[4], cnt);
-		base = __shfl_sync(0xffffffffu, base, 0);
+			b = atomicAdd(&S.misc[4], (uint32_t)__popc(starts));
+		return b;
+	};
+	warp_merge_plane(S.u.masks[p], reserve, [&](uint32_t b, int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
+		const uint32_t cnt = __popc(starts);
+		const uint32_t base = __shfl_sync(0xffffffffu, b, 0);
 		if (is_start) {
 			const int st = (int)((tmask >> lane) & 1u);
 			const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
@@ -816,7 +823,8 @@ __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 			if (!pc || pb >= w0 + kQuadBuf || pb + pc <= w0)
 				continue;
 			uint32_t n_all = 0, n_st[2] = {0, 0};
-			warp_merge_plane(S.u.masks[p], [&](int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
+			warp_merge_plane(S.u.masks[p], [](uint32_t) { return 0u; },
+			                 [&](uint32_t, int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
 				if (is_start) {
 					const int st = (int)((tmask >> lane) & 1u);
 					const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
