@@ -149,6 +149,12 @@ int cell_of_chunk(const hc_server *s, int cx, int cy, int cz) {
 
 uint32_t fill_voxels(const hc_request &r) { return r.size * r.size * r.size; }
 
+// Unloads a tick takes (besides max_loads_per_tick loads): an unload only drops a chunk, and a
+// player's move unloads a whole shell of the view at once. Staging per tick: unload positions
+// (3 x kUnloadsPerTick), then load positions (3 x L) and load slots (L).
+constexpr uint32_t kUnloadsPerTick = 4096;
+size_t stage_ints(uint32_t L) { return 3 * (size_t)kUnloadsPerTick + 4 * (size_t)L; }
+
 // Decides which queued requests the next tick takes, in arrival order, stopping at the first that
 // does not fit. A load or unload of a chunk that the tick already edits waits for the next tick,
 // since the device pass applies unloads and loads before edits; so does a second load or unload of
@@ -159,10 +165,10 @@ void admit(hc_server *s, TickSlot &t) {
 	uint32_t ne = 0, nl = 0, nu = 0;
 	t.reqs.clear();
 	t.freed.clear();
-	int32_t *unload_pos = t.h_stage;
-	int32_t *load_pos = t.h_stage + 3 * c.max_loads_per_tick;
-	int32_t *load_slot = t.h_stage + 6 * c.max_loads_per_tick;
 	const uint32_t L = c.max_loads_per_tick;
+	int32_t *unload_pos = t.h_stage;
+	int32_t *load_pos = t.h_stage + 3 * kUnloadsPerTick;
+	int32_t *load_slot = load_pos + 3 * L;
 	t.n_dchunks = t.n_bent = t.n_sent = 0;
 	t.h_doff[0] = 0, t.h_doff[L + 1] = 0;
 	while (!s->queue.empty()) {
@@ -199,7 +205,8 @@ void admit(hc_server *s, TickSlot &t) {
 			if (cell < 0 || (r.kind == HC_REQ_LOAD && (!r.blocks || !r.heights)) || bad_entries) {
 				status = kStatusRejected;
 			} else {
-				if (edited.count(cell) || moved.count(cell) || nl + nu + 1 > c.max_loads_per_tick)
+				if (edited.count(cell) || moved.count(cell) ||
+				    (r.kind == HC_REQ_LOAD ? nl + 1 > L : nu + 1 > kUnloadsPerTick))
 					break;
 				if (r.kind == HC_REQ_LOAD && s->cell_slot[cell] < 0 &&
 				    (t.n_bent + r.n_block_entries > kTickEntries || t.n_sent + r.n_sunlight_entries > kTickEntries))
@@ -257,8 +264,8 @@ hc_status enqueue_pass(hc_server *s, TickSlot &t) {
 	if (t.n_edits)
 		SV_CUDA(s, cudaMemcpyAsync(t.d_edits, t.h_edits, t.n_edits * sizeof(hc_edit), cudaMemcpyHostToDevice, s->ks));
 	if (t.n_loads + t.n_unloads)
-		SV_CUDA(s, cudaMemcpyAsync(t.d_stage, t.h_stage, 7 * L * sizeof(int32_t), cudaMemcpyHostToDevice, s->ks));
-	const int32_t *load_slot = t.h_stage + 6 * L;
+		SV_CUDA(s, cudaMemcpyAsync(t.d_stage, t.h_stage, stage_ints(L) * sizeof(int32_t), cudaMemcpyHostToDevice, s->ks));
+	const int32_t *load_slot = t.h_stage + 3 * kUnloadsPerTick + 3 * L;
 	for (uint32_t i = 0; i < t.n_loads; ++i) {
 		SV_CUDA(s, cudaMemcpyAsync(pool_blocks + (size_t)load_slot[i] * 32768, t.h_blocks + (size_t)i * 32768,
 		                           32768 * sizeof(uint16_t), cudaMemcpyHostToDevice, s->ks));
@@ -279,7 +286,8 @@ hc_status enqueue_pass(hc_server *s, TickSlot &t) {
 	if ((st = world_enqueue_deltas(s->world, t.d_dslot, t.d_doff, t.d_doff + L + 1, t.d_bent, t.d_sent, t.n_dchunks,
 	                               s->cs)) != HC_OK ||
 	    (st = world_enqueue_evict(s->world, t.d_stage, t.n_unloads, s->cs)) != HC_OK ||
-	    (st = world_enqueue_place(s->world, t.d_stage + 3 * L, t.d_stage + 6 * L, t.n_loads, s->cs)) != HC_OK ||
+	    (st = world_enqueue_place(s->world, t.d_stage + 3 * kUnloadsPerTick, t.d_stage + 3 * kUnloadsPerTick + 3 * L,
+	                              t.n_loads, s->cs)) != HC_OK ||
 	    (st = world_enqueue_edits(s->world, t.d_edits, t.n_edits, s->cs)) != HC_OK ||
 	    (t.n_edits && (st = world_enqueue_heights(s->world, s->cs)) != HC_OK))
 		return st;
@@ -483,8 +491,8 @@ hc_status hc_server_create(hc_ctx *ctx, const hc_world_desc *desc, uint32_t pool
 	for (TickSlot &t : s->ring) {
 		H((void **)&t.h_edits, E * sizeof(hc_edit));
 		A((void **)&t.d_edits, E * sizeof(hc_edit));
-		H((void **)&t.h_stage, 7 * L * sizeof(int32_t));
-		A((void **)&t.d_stage, 7 * L * sizeof(int32_t));
+		H((void **)&t.h_stage, stage_ints(L) * sizeof(int32_t));
+		A((void **)&t.d_stage, stage_ints(L) * sizeof(int32_t));
 		H((void **)&t.h_blocks, (size_t)L * 32768 * sizeof(uint16_t));
 		H((void **)&t.h_heights, (size_t)L * 1024);
 		H((void **)&t.h_counts, kWorldCountWords * sizeof(uint32_t));
@@ -510,7 +518,7 @@ hc_status hc_server_create(hc_ctx *ctx, const hc_world_desc *desc, uint32_t pool
 		if (e == cudaSuccess)
 			e = cudaEventCreate(&t.done);
 		if (e == cudaSuccess)
-			std::memset(t.h_stage, 0, 7 * L * sizeof(int32_t));
+			std::memset(t.h_stage, 0, stage_ints(L) * sizeof(int32_t));
 	}
 	for (cudaStream_t *q : {&s->cs, &s->ks, &s->ss})
 		if (e == cudaSuccess)

@@ -285,8 +285,8 @@ hc_status hc_world_remesh(hc_world *world, const hc_batch_arena *arena, int32_t 
  * 16-130) with its worker threads (client/src/WorldWorker.cpp:18-27) and LocalClient's chunk loader
  * (client/src/LocalClient.cpp:14-27). Requests arrive at any time (hc_server_submit); every tick
  * the server admits, in arrival order, the requests that fit the tick (edits, with a fill counted
- * as its voxels, up to max_edits_per_tick; loads and unloads up to max_loads_per_tick; a load
- * needs a free pool slot, and slots freed by unloads return once their tick completes) and runs
+ * as its voxels, up to max_edits_per_tick; loads up to max_loads_per_tick; unloads up to 4,096; a
+ * load needs a free pool slot, and slots freed by unloads return once their tick completes) and runs
  * one device pass for them: unloads, loads, edits, sunlight heights, then relight + remesh of every
  * chunk they marked (as hc_world_*). Up to `depth` passes are in flight; each has its own arena.
  * A load or unload of a chunk that an earlier request of the same tick edits waits for the next
@@ -298,7 +298,7 @@ typedef struct hc_server_config {
 	uint32_t tick_us;            /* tick period in microseconds */
 	uint32_t depth;              /* passes in flight, 1..8 */
 	uint32_t max_edits_per_tick; /* edits per tick, a fill counting as its voxels */
-	uint32_t max_loads_per_tick; /* loads + unloads per tick */
+	uint32_t max_loads_per_tick; /* loads per tick (a tick also takes up to 4,096 unloads) */
 	uint64_t arena_quads;        /* per pass in flight; a chunk that does not fit is remeshed by a later pass */
 	uint32_t arena_meshes;
 	uint32_t ctas_per_chunk;     /* SMs meshing one chunk together (hc_world_set_cluster); 0: 4 */

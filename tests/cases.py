@@ -61,6 +61,15 @@ def checker():
     return b, h
 
 
+def transparent_checker():
+    """3D glass/ice checkerboard: every cell face shows from both sides, 196,608 quads in the centre
+    chunk (more than the mesher keeps records for, so its emission merges planes again)."""
+    b, h = _blank()
+    for i in range(27):
+        b[i] = np.where((X + Y + Z) % 2 == 0, 9, 12).astype(np.uint16)
+    return b, h
+
+
 def glow(seed):
     """5% glowstone in half-filled stone: torch light across chunk borders; sun from random heights."""
     rng = np.random.default_rng(seed)

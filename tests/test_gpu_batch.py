@@ -40,6 +40,26 @@ def test_batch_matches_oracle(ctx, oracle, kind, mode):
     assert total == q
 
 
+@pytest.mark.parametrize("mode", [0, 17, 18, 19])
+def test_batch_most_quads_match_oracle(ctx, oracle, mode):
+    """The 196,608-quad chunk through each persistent variant (records past the shared buffer and
+    the global scratch: the emission merges again in windows)."""
+    import cases
+    from hypercraft_gb300 import batch
+    b, h = cases.transparent_checker()
+    pool = batch.Pool(ctx, 27)
+    pool.upload(0, np.stack(b), np.stack(h))
+    arena = batch.Arena(400_000, 64, 1)
+    plan = batch.BatchPlan(ctx, pool, np.arange(27, dtype=np.int32)[None, :], arena, mode)
+    plan.launch()
+    q, m, f = plan.result()
+    assert f == 0 and q == 196608
+    got, want = arena.chunk_meshes(0, arena.host()), oracle.mesh_chunk(b, h)
+    assert len(got) == len(want) and all(a == c for a, c in zip(got, want))
+    plan.close()
+    pool.close()
+
+
 def test_batch_matches_single_chunk_call(ctx):
     from hypercraft_gb300 import batch
     w = _small_world("mixture")

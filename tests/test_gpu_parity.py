@@ -52,6 +52,15 @@ def test_mesh_chunk_matches_oracle_random(ctx, oracle, seed):
             assert a == c
 
 
+def test_most_quads_match_oracle(ctx, oracle):
+    """196,608 quads: past the shared and global record buffers, so the emission merges planes again
+    in windows; the result still equals the oracle's."""
+    b, h = cases.transparent_checker()
+    mg, mo = ctx.mesh_chunk(b, h), oracle.mesh_chunk(b, h)
+    assert sum(len(m.vertices) for m in mo) // 4 == 196608
+    assert len(mg) == len(mo) and all(a == c for a, c in zip(mg, mo))
+
+
 def test_device_entry_point_matches_host_entry_point(ctx):
     import torch
     from hypercraft_gb300.mesher import MESH_DESC_DTYPE, meshes_from_descs
