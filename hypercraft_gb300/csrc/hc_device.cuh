@@ -244,11 +244,6 @@ struct Light4 {
 	uint32_t sun, torch, ao;
 };
 
-// v / n for a light4 counter n in 1..4 and v < 2^16 (sums of four 4-bit levels, times four): a
-// shift for 1, 2 and 4, and for 3 the multiply-high by ceil(2^17 / 3), exact on that range
-// (Granlund and Montgomery, "Division by invariant integers using multiplication", 1994). A plain
-// integer division here costs eight software divisions per face.
-__device__ __forceinline__ uint32_t div_small(uint32_t v, uint32_t n) { return n == 3 ? (v * 43691u) >> 17 : v >> (n >> 1); }
 
 // Index offsets of the same neighbours in the 34^3 class and light arrays (x + 34 z + 34^2 y).
 __host__ __device__ constexpr int cell_offset(int dx, int dy, int dz) { return dx + kCls * dz + kCls * kCls * dy; }
@@ -269,11 +264,15 @@ __constant__ int16_t c_ring_off[6][8] = {
      HC_O(1, -1, -1)}};
 #undef HC_O
 
+// A cell's sun and torch levels side by side, sun in bits 0-7 and torch in bits 16-23, so that one
+// addition sums both channels (four 4-bit levels times four stay below 256).
+__device__ __forceinline__ uint32_t light_pair(uint32_t cell) { return (cell & 0x0fu) | ((cell & 0xf0u) << 12); }
+
 __device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
 	const int base = cls_index(x, y, z);
 	const uint32_t cf = S.cell[base + c_front_off[face]];
 	const bool dp3 = id_direct(cf >> 8);
-	const uint32_t lf = cf & 0xffu;
+	const uint32_t pf = light_pair(cf);
 	uint32_t ring[8];
 #pragma unroll
 	for (int i = 0; i < 8; ++i)
@@ -288,23 +287,25 @@ __device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
 			const uint32_t c = ring[(2 * v + b) & 7];
 			ip[b] = id_indirect(c >> 8);
 			dp[b] = id_direct(c >> 8);
-			l[b] = c & 0xffu;
+			l[b] = light_pair(c);
 		}
 		const int blocked = !dp[0] + !dp[1] + !dp[2] + !dp3;
 		const uint32_t ao = ((!dp[0] && !dp[2]) || (!dp[1] && !dp3)) ? 0u : (uint32_t)(3 - blocked > 0 ? 3 - blocked : 0);
-		uint32_t counter = 1, sun = lf & 15u, torch = lf >> 4;
-		if (ip[0] || ip[2]) {
-#pragma unroll
-			for (int b = 0; b < 3; ++b)
-				if (ip[b]) {
-					++counter;
-					sun += l[b] & 15u;
-					torch += l[b] >> 4;
-				}
-		}
+		// the front cell, plus every light-passing side or corner cell when a side passes light
+		const bool any = ip[0] || ip[2];
+		const bool i0 = any && ip[0], i1 = any && ip[1], i2 = any && ip[2];
+		const uint32_t sum = (pf + (i0 ? l[0] : 0u) + (i1 ? l[1] : 0u) + (i2 ? l[2] : 0u)) << 2;
+		const uint32_t counter = 1u + i0 + i1 + i2;
+		// (sum << 2) / counter in both halves: a shift for 1, 2 and 4; for 3 the multiply-high by
+		// 171 / 512, exact for every value up to 240 (Granlund and Montgomery, "Division by invariant
+		// integers using multiplication", 1994), the sun product staying below bit 16. A plain
+		// integer division here would cost eight software divisions per face.
+		const uint32_t pr = sum * 171u;
+		const uint32_t q = counter == 3 ? (((pr >> 9) & 0x7fu) | (((pr >> 25) & 0x7fu) << 16))
+		                                : ((sum >> (counter >> 1)) & 0x00ff00ffu);
 		r.ao |= ao << (2 * v);
-		r.sun |= div_small(sun << 2, counter) << (8 * v);
-		r.torch |= div_small(torch << 2, counter) << (8 * v);
+		r.sun |= (q & 0xffu) << (8 * v);
+		r.torch |= (q >> 16) << (8 * v);
 	}
 	return r;
 }
