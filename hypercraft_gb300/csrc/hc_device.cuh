@@ -153,6 +153,7 @@ struct Smem {
 	uint8_t plane_owner[kPlanes]; // cluster form, in CTA 0: the CTA that took each face plane
 	uint8_t mine[kPlanes];        // the face planes this CTA took, in the order it took them
 	uint8_t order[kPlanes];       // the face planes by falling face count: the order they are taken in
+	uint8_t row_of[kWarps][32];   // per warp, key pass: the row whose faces start at each lane of a batch
 };
 
 __device__ __forceinline__ int cls_index(int x, int y, int z) { return ((y + 1) * kCls + (z + 1)) * kCls + (x + 1); }

@@ -544,7 +544,7 @@ __device__ void plane_count_one(Smem &S, int p);
 // the light keys are computed by full warps; a face's right neighbour is the next lane and its
 // upper neighbour sits in this batch or in the previous one.
 __device__ void plane_keys(Smem &S, const Split &sp) {
-	const int lane = threadIdx.x & 31;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	for (int p = claim_plane(S, sp); p < kPlanes; p = claim_plane(S, sp)) {
 		plane_complex_one(S, p);
 		uint32_t *mrow = S.u.masks[p][lane];
@@ -576,14 +576,17 @@ __device__ void plane_keys(Smem &S, const Split &sp) {
 			const uint32_t bend = ue < 32 ? be : total;
 			// this lane's face: compacted index f = b + lane. The batch starts at row ub's first face
 			// and every row holds at most 32 faces, so the rows of the batch that hold faces start
-			// at distinct lanes: lane j's row is the m-th of them, m = the row starts at or below j.
+			// at distinct lanes: lane j's row is the one that starts at the last start at or below j.
 			const uint32_t f = b + lane;
 			const bool has = f < bend;
 			const bool rin = lane >= ub && lane < ue && cnt > 0;
-			const uint32_t R = __ballot_sync(0xffffffffu, rin);
 			const uint32_t M = __reduce_or_sync(0xffffffffu, rin ? 1u << (start - b) : 0u);
 			const uint32_t upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
-			const int u = has ? nth_set_bit(R, (uint32_t)__popc(M & upto) - 1u) : 0;
+			if (rin) // each row of the batch records itself where its faces start
+				S.row_of[warp][start - b] = (uint8_t)lane;
+			__syncwarp();
+			const int u = has ? S.row_of[warp][31 - __clz(M & upto)] : 0;
+			__syncwarp();
 			const uint32_t su = __shfl_sync(0xffffffffu, start, u); // every lane takes part
 			const uint32_t k = has ? f - su : 0u;
 			const uint32_t Nu = __shfl_sync(0xffffffffu, N, u);
