@@ -557,50 +557,52 @@ __device__ __forceinline__ uint64_t light_bytes8(const uint32_t w[8], int g) {
 // edge bits, 32 rows (z) per word.
 __device__ void light_from_levels(Smem &S) {
 	uint8_t *light = light_bytes(S);
-	for (int row = threadIdx.x; row < kLt * kLt; row += kThreads) {
-		const int y = row / kLt - 1, z = row % kLt - 1;
-		const uint32_t *L = S.lvl[nb_index(0, y, z)];
-		const int ry = (y & 31) * 32 + (z & 31);
+	// one item per thread and round: the 34 x 34 rows (x in [0, 32)), then the 2 x 34 x 3 edge
+	// pieces (x = -1 or 32; z = -1, [0, 32) or 32), so that both kinds share the second round
+	constexpr int kRowItems = kLt * kLt, kItems = kRowItems + 2 * kLt * 3;
+	for (int it = threadIdx.x; it < kItems; it += kThreads) {
+		const uint32_t *src;
+		int stride;
+		int x = 0, y, zc = 1, z0 = 0;
+		if (it < kRowItems) {
+			y = it / kLt - 1;
+			const int z = it % kLt - 1;
+			src = S.lvl[nb_index(0, y, z)] + (y & 31) * 32 + (z & 31);
+			stride = kPlaneWords;
+		} else {
+			const int k = it - kRowItems, side = k / (kLt * 3), rem = k - side * (kLt * 3);
+			y = rem / 3 - 1, zc = rem % 3;
+			x = side ? kChunk : -1, z0 = zc == 0 ? -1 : (zc == 1 ? 0 : kChunk);
+			src = S.edg[nb_index(x, y, z0)] + (side ? 0 : 32) + (y & 31); // x = 0 or x = 31 bits over z
+			stride = 64;
+		}
 		uint32_t b[2][4];
 #pragma unroll
 		for (int c = 0; c < 2; ++c) {
 			uint32_t lv[kLevels];
 #pragma unroll
 			for (int u = 0; u < kLevels; ++u)
-				lv[u] = __ldg(L + (size_t)(c * kLevels + u) * kPlaneWords + ry);
+				lv[u] = __ldg(src + (size_t)(c * kLevels + u) * stride);
 			level_bits(lv, b[c]);
 		}
-		uint8_t *dst = light + 2 * (row * kLt + 1); // cell x = 0 of the row
 		const uint32_t w[8] = {b[0][0], b[0][1], b[0][2], b[0][3], b[1][0], b[1][1], b[1][2], b[1][3]};
+		if (zc == 1) { // 32 cells along x (a row) or along z (an x edge)
+			uint8_t *dst = it < kRowItems ? light + 2 * (it * kLt + 1) : light + 2 * lt_index(x, y, 0);
+			const int step = it < kRowItems ? 2 : 2 * kLt;
 #pragma unroll
-		for (int g = 0; g < 4; ++g) {
-			const uint64_t v = light_bytes8(w, g);
+			for (int g = 0; g < 4; ++g) {
+				const uint64_t v = light_bytes8(w, g);
 #pragma unroll
-			for (int j = 0; j < 8; ++j)
-				dst[2 * (8 * g + j)] = (uint8_t)(v >> (8 * j));
-		}
-	}
-	for (int k = threadIdx.x; k < 2 * kLt * 3; k += kThreads) {
-		const int side = k / (kLt * 3), rem = k - side * (kLt * 3), y = rem / 3 - 1, zc = rem % 3;
-		const int x = side ? kChunk : -1, z0 = zc == 0 ? -1 : (zc == 1 ? 0 : kChunk);
-		const uint32_t *E = S.edg[nb_index(x, y, z0)] + (side ? 0 : 32) + (y & 31); // x = 0 or x = 31 bits
-		uint32_t b[2][4];
-#pragma unroll
-		for (int c = 0; c < 2; ++c) {
-			uint32_t lv[kLevels];
-#pragma unroll
-			for (int u = 0; u < kLevels; ++u)
-				lv[u] = __ldg(E + (size_t)(c * kLevels + u) * 64);
-			level_bits(lv, b[c]);
-		}
-		const int zlo = zc == 1 ? 0 : z0, zhi = zc == 1 ? kChunk : z0 + 1;
-		for (int z = zlo; z < zhi; ++z) {
-			const int bz = z & 31;
+				for (int j = 0; j < 8; ++j)
+					dst[step * (8 * g + j)] = (uint8_t)(v >> (8 * j));
+			}
+		} else { // the corner cell z = -1 (bit 31 of the -z chunk) or z = 32 (bit 0 of the +z chunk)
+			const int bz = z0 & 31;
 			uint32_t v = 0;
 #pragma unroll
-			for (int bit = 0; bit < 4; ++bit)
-				v |= ((b[0][bit] >> bz) & 1u) << bit | ((b[1][bit] >> bz) & 1u) << (bit + 4);
-			light[2 * lt_index(x, y, z)] = (uint8_t)v;
+			for (int bit = 0; bit < 8; ++bit)
+				v |= ((w[bit] >> bz) & 1u) << bit;
+			light[2 * lt_index(x, y, z0)] = (uint8_t)v;
 		}
 	}
 }
