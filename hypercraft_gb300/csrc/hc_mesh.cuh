@@ -39,8 +39,9 @@ enum : int { kClaimComplex = 12, kClaimKeys = 13, kMine = 15 }; // S.misc counte
 // Orders the face planes by falling weight (visible faces and complex candidates, a tie to the
 // lower plane) into S.order, so that the key pass takes the heaviest planes first and its last
 // planes are light ones (longest-first scheduling). Weights sit in seg_base, unused until the scan.
-// Every CTA of a cluster computes the same order from the same masks.
-__device__ void order_planes(Smem &S) {
+// Every CTA of a cluster computes the same order from the same masks. Returns how many planes have
+// any face: the rest are left out of the key pass (their counts stay 0; their owner is CTA 0).
+__device__ int order_planes(Smem &S) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	uint32_t *weight = &S.seg_base[0][0];
 	for (int p = warp; p < kPlanes; p += kWarps) {
@@ -58,27 +59,28 @@ __device__ void order_planes(Smem &S) {
 			rank += (wq > w) || (wq == w && q < p);
 		}
 		S.order[rank] = (uint8_t)p;
+		if (w == 0)
+			S.plane_owner[p] = 0;
 	}
-	__syncthreads();
+	return __syncthreads_count(threadIdx.x < kPlanes && weight[threadIdx.x] > 0);
 }
 
 // Next face plane for the calling warp's key pass. In a cluster the planes are taken from one
 // counter in CTA 0, so a heavy plane does not hold up a CTA with a fixed share; the taker records
 // the plane as its own (count and emission run where its masks are) and in CTA 0's owner table.
-__device__ __forceinline__ int claim_plane(Smem &S, const Split &sp) {
+__device__ __forceinline__ int claim_plane(Smem &S, const Split &sp, int live) {
 	int p = 0;
 	if ((threadIdx.x & 31) == 0) {
 		if (sp.c > 1) {
 			cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
 			p = (int)atomicAdd(cl.map_shared_rank(&S.misc[kClaimKeys], 0), 1u);
+			p = p < live ? (int)S.order[p] : kPlanes;
 			if (p < kPlanes) {
-				p = S.order[p];
 				cl.map_shared_rank(&S.plane_owner[0], 0)[p] = (uint8_t)sp.rank;
 			}
 		} else {
 			p = (int)atomicAdd(&S.misc[kClaimKeys], 1u);
-			if (p < kPlanes)
-				p = S.order[p];
+			p = p < live ? (int)S.order[p] : kPlanes;
 		}
 		if (p < kPlanes)
 			S.mine[atomicAdd(&S.misc[kMine], 1u)] = (uint8_t)p;
@@ -543,9 +545,9 @@ __device__ void plane_count_one(Smem &S, int p);
 // faces of a plane are taken in batches of whole rows (at most 32 faces), one face per lane, so
 // the light keys are computed by full warps; a face's right neighbour is the next lane and its
 // upper neighbour sits in this batch or in the previous one.
-__device__ void plane_keys(Smem &S, const Split &sp) {
+__device__ void plane_keys(Smem &S, const Split &sp, int live) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int p = claim_plane(S, sp); p < kPlanes; p = claim_plane(S, sp)) {
+	for (int p = claim_plane(S, sp, live); p < kPlanes; p = claim_plane(S, sp, live)) {
 		plane_complex_one(S, p);
 		uint32_t *mrow = S.u.masks[p][lane];
 		const uint32_t N = mrow[0];
@@ -670,17 +672,21 @@ __device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], G &&on_
 		const bool in_run = (live >> lane) & 1u, is_start = (starts >> lane) & 1u;
 		const uint32_t after = lane == 31 ? 0u : (cont >> (lane + 1));
 		const int rem = __ffs(~after); // lanes from this one to the end of its run
-		// rows below u this column can grow over, then the minimum over the rest of the run
-		int dl = in_run ? __ffs(~(Dc >> u)) - 1 : 32;
+		// rows below u this column can grow over, then the minimum over the rest of the run (all
+		// heights are 1 when no cell of the row's runs equals the one below it)
+		int h = 1;
+		if (__any_sync(0xffffffffu, in_run && ((Dc >> u) & 1u))) {
+			int dl = in_run ? __ffs(~(Dc >> u)) - 1 : 32;
 #pragma unroll
-		for (int d = 1; d < 32; d <<= 1) {
-			const int o = __shfl_down_sync(0xffffffffu, dl, d);
-			if (d < rem)
-				dl = min(dl, o);
+			for (int d = 1; d < 32; d <<= 1) {
+				const int o = __shfl_down_sync(0xffffffffu, dl, d);
+				if (d < rem)
+					dl = min(dl, o);
+			}
+			h = __shfl_sync(0xffffffffu, dl, 31 - __clz(starts & upto)) + 1; // the run's start
+			if (in_run)
+				Cc |= (h == 32 ? 0xffffffffu : ((1u << h) - 1u)) << u;
 		}
-		const int h = __shfl_sync(0xffffffffu, dl, 31 - __clz(starts & upto)) + 1; // the run's start
-		if (in_run)
-			Cc |= (h == 32 ? 0xffffffffu : ((1u << h) - 1u)) << u;
 		on_row(token, u, starts, Tu, is_start, rem, h);
 	}
 }
@@ -981,10 +987,10 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		__syncthreads();
 		plane_visibility(S);
 		__syncthreads();
-		order_planes(S);
+		const int live = order_planes(S);
 		if (sp.c > 1) // CTA 0's plane counter was reset for this chunk before any CTA takes from it
 			cooperative_groups::this_cluster().sync();
-		plane_keys(S, sp); // with each plane's quad count and records
+		plane_keys(S, sp, live); // with each plane's quad count and records
 		if (tid == 0) {
 			S.seg_cnt[0][0] = to;
 			S.seg_cnt[1][0] = tt;
