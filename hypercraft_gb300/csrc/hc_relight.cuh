@@ -396,6 +396,7 @@ constexpr int kLevels = 15;
 constexpr size_t kLevelSlotWords = (size_t)2 * kLevels * kPlaneWords; // per chunk: 2 channels x 15 levels
 constexpr size_t kEdgeSlotWords = (size_t)2 * kLevels * 2 * 32;       // per chunk: x = 0 and x = 31 bits
 constexpr int kLightThreads = 256;                                     // one block per chunk
+constexpr int kLightRows = kPlaneWords / kLightThreads;                // rows per thread
 
 struct LightPass {
 	const int32_t *slots;   // batch chunk -> pool slot
@@ -425,85 +426,107 @@ __device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
 	           mux(b[2], mux(b[1], s[6], s[4]), mux(b[1], s[2], s[0])));
 }
 
-// Level t of every batch chunk, one block per chunk, no shared memory and no block barrier: warp
-// w takes the y layers [4w, 4w + 4), lane z the rows (y, z) of both channels. A row's y neighbours
-// are the thread's own rows or one row above and below its range, its z neighbours the next lanes
-// (shuffles), its x neighbours the row word's own shifts; at the chunk's faces the six face
-// neighbours' level t + 1 rows and x-edge words. Every row load and store is coalesced over z, and
-// all of a thread's loads are independent. Also writes the row edge bits that the x neighbours read
-// at the next level: word y = bit z of cells (x = 0, y, z), word 32 + y = cells (x = 31, y, z).
+// Level t of every batch chunk, one block per chunk: the chunk's level t + 1 rows and the rows and
+// edge bits of its six face neighbours that touch it are staged in shared memory with coalesced
+// loads (the chunk's own rows are requested before its neighbour list arrives), then each thread
+// dilates kLightRows rows of both channels. Also writes the row edge bits that the x neighbours
+// read at the next level.
 __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevTables T, int t) {
-	constexpr int kY = kChunk / (kLightThreads / 32); // y layers per warp
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, z = lane, y0 = warp * kY;
+	__shared__ __align__(16) uint32_t prev[2][kPlaneWords];
+	__shared__ uint32_t side[2][6][32]; // per channel: -x hi edge, +x lo edge, -y rows, +y rows, -z rows, +z rows
+	__shared__ int s_nb[6];
+	__shared__ int32_t s_slot;
+	const int tid = threadIdx.x, lane = tid & 31;
 	const int i = blockIdx.x;
-	const int32_t slot = __ldg(L.slots + i);
-	const uint32_t *P = L.planes + (size_t)slot * kPlaneStride;
-	uint32_t s[2][kY];
-	if (t == kLevels) { // the seeds of level 15: sunlit cells, emitters of level 15
+	constexpr int kQ = 2 * kPlaneWords / 4 / kLightThreads; // uint4 of the two channels per thread
+	uint4 own[kQ];
+	if (t < kLevels) {
 #pragma unroll
-		for (int k = 0; k < kY; ++k) {
-			s[0][k] = __ldg(P + kPlaneSun * kPlaneWords + (y0 + k) * 32 + z);
-			s[1][k] = __ldg(P + kPlaneT15 * kPlaneWords + (y0 + k) * 32 + z);
+		for (int q = 0; q < kQ; ++q) {
+			const int j = tid + q * kLightThreads, c = j / (kPlaneWords / 4), o = j % (kPlaneWords / 4);
+			own[q] = __ldg(reinterpret_cast<const uint4 *>(level_plane(L, i, c, t + 1)) + o);
 		}
-	} else {
-		const int nb = lane < 6 ? __ldg(L.nb6 + 6 * (size_t)i + lane) : -1;
-		const int nxm = __shfl_sync(0xffffffffu, nb, 0), nxp = __shfl_sync(0xffffffffu, nb, 1);
-		const int nym = __shfl_sync(0xffffffffu, nb, 2), nyp = __shfl_sync(0xffffffffu, nb, 3);
-		const int nzm = __shfl_sync(0xffffffffu, nb, 4), nzp = __shfl_sync(0xffffffffu, nb, 5);
-		uint32_t pass[kY];
+	}
+	if (tid < 6)
+		s_nb[tid] = __ldg(L.nb6 + 6 * i + tid);
+	if (tid == 6)
+		s_slot = __ldg(L.slots + i);
+	__syncthreads();
+	const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
+	if (t < kLevels) {
+		for (int j = tid; j < 2 * 6 * 32; j += kLightThreads) {
+			const int c = j / 192, f = (j / 32) % 6, k = j & 31, nb = s_nb[f];
+			uint32_t v = 0;
+			if (nb >= 0) {
+				if (f == 0)
+					v = __ldg(level_edges(L, nb, c, t + 1) + 32 + k); // x = 31 bits of the -x neighbour
+				else if (f == 1)
+					v = __ldg(level_edges(L, nb, c, t + 1) + k); // x = 0 bits of the +x neighbour
+				else if (f == 2)
+					v = __ldg(level_plane(L, nb, c, t + 1) + 31 * 32 + k); // its y = 31 row at z = k
+				else if (f == 3)
+					v = __ldg(level_plane(L, nb, c, t + 1) + k); // y = 0, z = k
+				else if (f == 4)
+					v = __ldg(level_plane(L, nb, c, t + 1) + k * 32 + 31); // z = 31 row at y = k
+				else
+					v = __ldg(level_plane(L, nb, c, t + 1) + k * 32); // z = 0, y = k
+			}
+			side[c][f][k] = v;
+		}
 #pragma unroll
-		for (int k = 0; k < kY; ++k)
-			pass[k] = __ldg(P + kPlanePass * kPlaneWords + (y0 + k) * 32 + z);
+		for (int q = 0; q < kQ; ++q) {
+			const int j = tid + q * kLightThreads, c = j / (kPlaneWords / 4), o = j % (kPlaneWords / 4);
+			reinterpret_cast<uint4 *>(prev[c])[o] = own[q];
+		}
+	}
+	uint32_t pass[kLightRows], lows[kLightRows], s[kLightRows][2];
 #pragma unroll
-		for (int c = 0; c < 2; ++c) {
-			const uint32_t *prev = level_plane(L, i, c, t + 1);
-			uint32_t me[kY + 2]; // rows y0 - 1 .. y0 + kY at z, level t + 1 (0 outside the batch)
+	for (int k = 0; k < kLightRows; ++k) {
+		const int r = tid + k * kLightThreads;
+		pass[k] = __ldg(P + kPlanePass * kPlaneWords + r);
+		lows[k] = __ldg(P + kPlaneLowOff + (r >> 5));
+		if (t == kLevels) {
+			s[k][0] = __ldg(P + kPlaneSun * kPlaneWords + r);
+			s[k][1] = __ldg(P + kPlaneT15 * kPlaneWords + r);
+		}
+	}
+	__syncthreads();
+	if (t < kLevels) {
 #pragma unroll
-			for (int k = 0; k < kY; ++k)
-				me[k + 1] = __ldg(prev + (y0 + k) * 32 + z);
-			me[0] = y0 > 0 ? __ldg(prev + (y0 - 1) * 32 + z)
-			               : (nym >= 0 ? __ldg(level_plane(L, nym, c, t + 1) + 31 * 32 + z) : 0u);
-			me[kY + 1] = y0 + kY < kChunk ? __ldg(prev + (y0 + kY) * 32 + z)
-			                              : (nyp >= 0 ? __ldg(level_plane(L, nyp, c, t + 1) + z) : 0u);
-			// per layer of the range: the -z and +z neighbours' rows (lanes 0 .. kY - 1 load them)
-			// and the x neighbours' edge words (bit z of cells x = -1 and x = 32)
-			const int ly = y0 + (lane & (kY - 1));
-			const uint32_t zm = lane < kY && nzm >= 0 ? __ldg(level_plane(L, nzm, c, t + 1) + ly * 32 + 31) : 0u;
-			const uint32_t zp = lane < kY && nzp >= 0 ? __ldg(level_plane(L, nzp, c, t + 1) + ly * 32) : 0u;
-			const uint32_t xm = lane < kY && nxm >= 0 ? __ldg(level_edges(L, nxm, c, t + 1) + 32 + ly) : 0u;
-			const uint32_t xp = lane < kY && nxp >= 0 ? __ldg(level_edges(L, nxp, c, t + 1) + ly) : 0u;
+		for (int k = 0; k < kLightRows; ++k) {
+			const int r = tid + k * kLightThreads, y = r >> 5, z = r & 31;
 #pragma unroll
-			for (int k = 0; k < kY; ++k) {
-				const uint32_t cur = me[k + 1];
-				const uint32_t up = __shfl_up_sync(0xffffffffu, cur, 1), dn = __shfl_down_sync(0xffffffffu, cur, 1);
-				const uint32_t zmk = __shfl_sync(0xffffffffu, zm, k), zpk = __shfl_sync(0xffffffffu, zp, k);
-				const uint32_t xmk = __shfl_sync(0xffffffffu, xm, k), xpk = __shfl_sync(0xffffffffu, xp, k);
-				uint32_t d = (cur << 1) | (cur >> 1) | ((xmk >> z) & 1u) | (((xpk >> z) & 1u) << 31);
-				d |= me[k] | me[k + 2] | (z > 0 ? up : zmk) | (z < 31 ? dn : zpk);
-				s[c][k] = cur | (pass[k] & d);
+			for (int c = 0; c < 2; ++c) {
+				const uint32_t me = prev[c][r];
+				uint32_t d = (me << 1) | (me >> 1);
+				d |= (side[c][0][r >> 5] >> (r & 31)) & 1u;
+				d |= ((side[c][1][r >> 5] >> (r & 31)) & 1u) << 31;
+				d |= y > 0 ? prev[c][r - 32] : side[c][2][z];
+				d |= y < 31 ? prev[c][r + 32] : side[c][3][z];
+				d |= z > 0 ? prev[c][r - 1] : side[c][4][y];
+				d |= z < 31 ? prev[c][r + 1] : side[c][5][y];
+				s[k][c] = me | (pass[k] & d);
 			}
 		}
 	}
-	// emitters below level 15 (rows flagged in the chunk planes) light their cells from their level
-	const uint32_t lows = __ldg(P + kPlaneLowOff + y0 + (lane & (kY - 1)));
 #pragma unroll
-	for (int k = 0; k < kY; ++k) {
-		const int y = y0 + k;
-		if ((__shfl_sync(0xffffffffu, lows, k) >> z) & 1u) {
-			const uint16_t *row = L.blocks + (size_t)slot * 32768 + (y * 32 + z) * 32;
+	for (int k = 0; k < kLightRows; ++k) {
+		const int r = tid + k * kLightThreads;
+		if ((lows[k] >> (r & 31)) & 1u) { // emitters below level 15 in this row
+			const uint16_t *row = L.blocks + (size_t)s_slot * 32768 + r * 32;
 			for (int x = 0; x < 32; ++x)
 				if (T.classes[T.class_of[row[x]]].light >= t)
-					s[1][k] |= 1u << x;
+					s[k][1] |= 1u << x;
 		}
 #pragma unroll
 		for (int c = 0; c < 2; ++c) {
 			uint32_t *out = L.levels + (size_t)i * kLevelSlotWords + (size_t)(c * kLevels + t - 1) * kPlaneWords;
-			out[y * 32 + z] = s[c][k];
-			const uint32_t lo = __ballot_sync(0xffffffffu, s[c][k] & 1u), hi = __ballot_sync(0xffffffffu, s[c][k] >> 31);
+			out[r] = s[k][c];
+			const uint32_t lo = __ballot_sync(0xffffffffu, s[k][c] & 1u), hi = __ballot_sync(0xffffffffu, s[k][c] >> 31);
 			if (lane == 0) {
 				uint32_t *e = L.edges + (size_t)i * kEdgeSlotWords + (size_t)(c * kLevels + t - 1) * 64;
-				e[y] = lo;
-				e[32 + y] = hi;
+				e[r >> 5] = lo;
+				e[32 + (r >> 5)] = hi;
 			}
 		}
 	}
