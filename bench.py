@@ -416,8 +416,10 @@ def ours(args):
                                       "mesh": float(stages[2])},
                          "algorithmic_bytes_per_launch": algo_bytes},
             "serving": serving,
-            # per step the plan's graph runs planes, 15 light levels (light-pass variant only) and the mesher
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * (17 if variant == 0 else 2),
+            # per step the plan's graph runs the plane refresh, the blank test (one-CTA variants), 15 light
+            # levels (light-pass variant only) and the mesher
+            "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": args.steps * (18 if variant == 0 else (3 if variant == 1 else 2)),
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -57,6 +57,33 @@ __global__ void __launch_bounds__(256) k_planes_pool(const uint16_t *pool_blocks
 	}
 }
 
+// Blank test of every chunk of a batch ahead of the mesher, one warp per chunk, from the layer
+// summaries of the chunk and its six face neighbours (as stage_classes does at its start): the
+// mesher then skips blank chunks without staging or prefetching them. A chunk with a bad
+// neighbour slot is left to the mesher, which reports it.
+__global__ void __launch_bounds__(256) k_blank_items(const uint32_t *planes, uint32_t pool_cap, const int32_t *nbr,
+                                                     uint32_t n, uint8_t *blank) {
+	const uint32_t i = blockIdx.x * 8 + (threadIdx.x >> 5);
+	const int lane = threadIdx.x & 31;
+	if (i >= n)
+		return;
+	const int32_t s = lane < 27 ? __ldg(nbr + (size_t)i * 27 + lane) : 0;
+	const bool bad = __any_sync(0xffffffffu, lane < 27 && (s < 0 || (uint32_t)s >= pool_cap));
+	const auto layers = [&](int k) { // lane's layer word of neighbour k
+		const int32_t sk = __shfl_sync(0xffffffffu, s, k);
+		return bad ? 0u : __ldg(planes + (size_t)sk * kPlaneStride + kPlaneLayerOff + lane);
+	};
+	const uint32_t mine = layers(26), xm = layers(nb_index(-1, 0, 0)), xp = layers(nb_index(kChunk, 0, 0));
+	const uint32_t zm = layers(nb_index(0, 0, -1)), zp = layers(nb_index(0, 0, kChunk));
+	const uint32_t ym = __shfl_sync(0xffffffffu, layers(nb_index(0, -1, 0)), 31);
+	const uint32_t yp = __shfl_sync(0xffffffffu, layers(nb_index(0, kChunk, 0)), 0);
+	const uint32_t open = (mine & kLayerOpen) | (xm & kLayerOpenX31) | (xp & kLayerOpenX0) | (zm & kLayerOpenZ31) |
+	                      (zp & kLayerOpenZ0) | ((ym | yp) & kLayerOpen);
+	const bool is_blank = !bad && (!__any_sync(0xffffffffu, mine & kLayerContent) || !__any_sync(0xffffffffu, open));
+	if (lane == 0)
+		blank[i] = is_blank;
+}
+
 // Planes of the 27 chunks of a single-chunk call.
 __global__ void __launch_bounds__(256) k_planes_refs(Refs27 refs, DevTables T, uint32_t *planes) {
 	__shared__ DevClass cls[256];
@@ -170,7 +197,8 @@ __device__ __forceinline__ void prefetch_item(const uint16_t *pool_blocks, const
 __global__ void __launch_bounds__(kThreads, 1)
     k_mesh_batch(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
                  const int32_t *nbr, uint32_t n, const uint32_t *n_dev, unsigned int *work, unsigned int *failed,
-                 DevTables T, Arena A, const uint32_t *levels, const uint32_t *edges, const int32_t *nbr_local) {
+                 DevTables T, Arena A, const uint32_t *levels, const uint32_t *edges, const int32_t *nbr_local,
+                 const uint8_t *item_blank) {
 	Smem &S = smem();
 	__shared__ uint32_t s_next;
 	if (n_dev) // the batch length is known on the device only (a world remesh)
@@ -187,9 +215,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 			s_next = atomicAdd(work, 1u);
 		__syncthreads();
 		const uint32_t next = s_next;
-		if (next < n)
+		if (next < n && !(item_blank && item_blank[next]))
 			prefetch_item(pool_blocks, pool_planes, pool_cap, nbr, next, levels, nbr_local);
-		if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, levels, edges, nbr_local)) {
+		if (item_blank && item_blank[item]) { // no quad: the results a blank chunk gets
+			if (threadIdx.x < 5)
+				A.results[5 * (size_t)item + threadIdx.x] = threadIdx.x == 4 ? kChunkOk : 0u;
+		} else if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, levels, edges, nbr_local)) {
 			mesh_chunk_cta(S, T, A, item);
 			if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
 				atomicAdd(failed, 1u);
@@ -328,6 +359,7 @@ struct hc_batch_plan {
 	// batch light pass (persistent form): the distinct slots are the batch's chunks 0..n_slots-1
 	int32_t *d_nb6 = nullptr;       // per batch chunk: its six face neighbours in the batch, or -1
 	int32_t *d_nbr_local = nullptr; // n x 27: the neighbour table in batch chunk numbers
+	uint8_t *d_blank = nullptr;     // per chunk to mesh: blank (no quad), from the layer summaries
 	uint32_t *d_levels = nullptr;   // per batch chunk: 2 channels x 15 level planes
 	uint32_t *d_edges = nullptr;    // per batch chunk: their x = 0 and x = 31 bits
 	unsigned long long *d_state = nullptr; // quad cursor, mesh cursor, work counter, failed chunks
@@ -931,6 +963,10 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		                                     p->pool->d_planes);
 		HC_CUDA(ctx, cudaGetLastError());
 	}
+	if (p->d_blank && p->n_slots && p->variant < HC_VARIANT_CLUSTER2) {
+		k_blank_items<<<(p->n + 7) / 8, 256, 0, st>>>(p->pool->d_planes, p->pool->capacity, p->nbr, p->n, p->d_blank);
+		HC_CUDA(ctx, cudaGetLastError());
+	}
 	if ((s = stage_mark(p, 1, st)) != HC_OK)
 		return s;
 	const bool light_pass = p->variant == HC_VARIANT_LIGHT_PASS && p->d_levels;
@@ -959,7 +995,7 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(
 		    p->pool->d_blocks, p->pool->d_heights, p->pool->d_planes, p->pool->capacity, p->nbr, p->n, nullptr, work,
 		    failed, tables(ctx), A, light_pass ? p->d_levels : nullptr, light_pass ? p->d_edges : nullptr,
-		    light_pass ? p->d_nbr_local : nullptr);
+		    light_pass ? p->d_nbr_local : nullptr, p->d_blank);
 		HC_CUDA(ctx, cudaGetLastError());
 	} else {
 		for (uint32_t i = 0; i < p->n; ++i) {
@@ -1039,6 +1075,8 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 		                                                  p->cluster_grid[HC_VARIANT_CLUSTER4]));
 		e = cudaMalloc(&p->d_spill, (size_t)ctas * kSpillRecs * sizeof(uint2));
 	}
+	if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT) // the one-CTA persistent kernel skips blank chunks
+		e = cudaMalloc(&p->d_blank, n);
 	for (int i = 0; i < 4 && e == cudaSuccess; ++i)
 		e = cudaEventCreate(&p->stage_ev[i]);
 	if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT) {
@@ -1152,6 +1190,7 @@ void hc_batch_plan_destroy(hc_batch_plan *plan) {
 	cudaFree(plan->d_edges);
 	cudaFree(plan->d_state);
 	cudaFree(plan->d_spill);
+	cudaFree(plan->d_blank);
 	cudaFreeHost(plan->h_state);
 	delete plan;
 }
@@ -1338,7 +1377,7 @@ hc_status world_enqueue_remesh(hc_world *w, const hc_batch_arena *arena, cudaStr
 	} else {
 		k_mesh_batch<<<w->sms, kThreads, ctx->smem_bytes, st>>>(
 		    w->pool->d_blocks, w->pool->d_heights, w->pool->d_planes, w->pool->capacity, w->d_nbr, 0u,
-		    w->d_counts + kCountRemesh, work, failed, tables(ctx), A, nullptr, nullptr, nullptr);
+		    w->d_counts + kCountRemesh, work, failed, tables(ctx), A, nullptr, nullptr, nullptr, nullptr);
 	}
 	HC_CUDA(ctx, cudaGetLastError());
 	k_requeue<<<list_grid(w), 256, 0, st>>>(W, w->d_list, A.results);
@@ -1873,7 +1912,7 @@ extern "C" hc_status hc_mesh_batch_noalloc(const uint16_t *pool_blocks, const in
 		        results};
 		k_mesh_batch<<<D.sms, kThreads, sizeof(Smem), st>>>(pool_blocks, pool_heights, nullptr, pool_capacity, neighbours,
 		                                                     n, nullptr, state + 4, state + 5, DevTables{D.class_of, D.classes}, A,
-		                                                     nullptr, nullptr, nullptr);
+		                                                     nullptr, nullptr, nullptr, nullptr);
 		e = cudaGetLastError();
 	}
 	uint32_t host_state[kNoAllocStateWords];
