@@ -60,6 +60,24 @@ def test_batch_most_quads_match_oracle(ctx, oracle, mode):
     pool.close()
 
 
+def test_stage_times_and_blank_chunks(ctx):
+    """The plan's in-graph stage events time every stage of the light-pass variant, and chunks the
+    blank test skips get the empty result (no quad, status ok)."""
+    from hypercraft_gb300 import batch
+    w = _small_world("mixture")
+    rw = batch.upload_world(ctx, w)
+    n = len(rw.chunks)
+    arena = batch.Arena(3_000_000, 4096, n)
+    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, batch.PERSISTENT)
+    plan.launch()
+    planes_ms, light_ms, mesh_ms = plan.stage_ms()
+    assert planes_ms > 0 and light_ms > 0 and mesh_ms > 0
+    res = arena.results_host(n).reshape(n, 5)
+    blank = [i for i in range(n) if not (w.blocks[rw.chunks[i]] != 0).any()]  # all-air chunks
+    assert blank, "the mixture holds all-air chunks"
+    assert (res[blank] == 0).all()
+
+
 def test_batch_matches_single_chunk_call(ctx):
     from hypercraft_gb300 import batch
     w = _small_world("mixture")
