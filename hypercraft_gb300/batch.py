@@ -51,6 +51,7 @@ def _bind(lib):
     lib.hc_batch_plan_launch.argtypes = [vp, vp]
     lib.hc_batch_plan_result.argtypes = [vp, P(ctypes.c_uint64), P(ctypes.c_uint32), P(ctypes.c_uint32)]
     lib.hc_batch_plan_download.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint32, vp, vp, vp, vp]
+    lib.hc_batch_plan_download_async.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint32, vp, vp, vp, vp, vp]
     lib.hc_batch_plan_variant.argtypes = [vp, P(ctypes.c_int), vp]
     lib.hc_batch_plan_stage_ms.argtypes = [vp, vp]
     lib._batch_bound = True

@@ -1228,14 +1228,14 @@ hc_status hc_batch_plan_result(hc_batch_plan *plan, uint64_t *quads, uint32_t *m
 	           : HC_OK;
 }
 
-hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t meshes, uint32_t *vertices,
-                                 uint16_t *indices, hc_mesh_desc *mesh_descs, uint32_t *results) {
+hc_status hc_batch_plan_download_async(hc_batch_plan *plan, uint64_t quads, uint32_t meshes, uint32_t *vertices,
+                                       uint16_t *indices, hc_mesh_desc *mesh_descs, uint32_t *results, void *stream) {
 	if (!plan)
 		return HC_ERR_INVALID_ARG;
 	hc_ctx *ctx = plan->ctx;
 	if (quads > plan->arena.quad_capacity || meshes > plan->arena.mesh_capacity)
 		return fail(ctx, HC_ERR_INVALID_ARG, "download beyond the arena");
-	cudaStream_t st = plan->last ? plan->last : ctx->stream;
+	cudaStream_t st = stream ? (cudaStream_t)stream : (plan->last ? plan->last : ctx->stream);
 	HC_CUDA(ctx, cudaSetDevice(ctx->device));
 	if (vertices && quads)
 		HC_CUDA(ctx, cudaMemcpyAsync(vertices, plan->arena.vertices, quads * 4 * sizeof(uint2), cudaMemcpyDeviceToHost, st));
@@ -1247,7 +1247,15 @@ hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t m
 	if (results)
 		HC_CUDA(ctx, cudaMemcpyAsync(results, plan->arena.results, (size_t)plan->n * 5 * sizeof(uint32_t),
 		                             cudaMemcpyDeviceToHost, st));
-	HC_CUDA(ctx, cudaStreamSynchronize(st));
+	return HC_OK;
+}
+
+hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t meshes, uint32_t *vertices,
+                                 uint16_t *indices, hc_mesh_desc *mesh_descs, uint32_t *results) {
+	const hc_status s = hc_batch_plan_download_async(plan, quads, meshes, vertices, indices, mesh_descs, results, nullptr);
+	if (s != HC_OK)
+		return s;
+	HC_CUDA(plan->ctx, cudaStreamSynchronize(plan->last ? plan->last : plan->ctx->stream));
 	return HC_OK;
 }
 

@@ -200,6 +200,11 @@ hc_status hc_batch_plan_result(hc_batch_plan *plan, uint64_t *quads, uint32_t *m
  * Any destination may be NULL to skip it. Synchronous. */
 hc_status hc_batch_plan_download(hc_batch_plan *plan, uint64_t quads, uint32_t meshes, uint32_t *vertices,
                                  uint16_t *indices, hc_mesh_desc *mesh_descs, uint32_t *results);
+/* The same copies enqueued on `stream` (NULL = the stream of the last launch) without waiting:
+ * with pinned destinations a client overlaps one batch's download with the next batch's upload
+ * and meshing (two pools and plans in flight). No counterpart in the reference. */
+hc_status hc_batch_plan_download_async(hc_batch_plan *plan, uint64_t quads, uint32_t meshes, uint32_t *vertices,
+                                       uint16_t *indices, hc_mesh_desc *mesh_descs, uint32_t *results, void *stream);
 
 
 

@@ -78,6 +78,28 @@ def test_stage_times_and_blank_chunks(ctx):
     assert (res[blank] == 0).all()
 
 
+def test_async_download_matches_download(ctx):
+    """hc_batch_plan_download_async on a stream gives the words hc_batch_plan_download gives."""
+    import torch
+    from hypercraft_gb300 import batch
+    w = _small_world("scale")
+    rw = batch.upload_world(ctx, w)
+    n = len(rw.chunks)
+    arena = batch.Arena(3_000_000, 4096, n)
+    plan = batch.BatchPlan(ctx, rw.pool, rw.neighbours, arena, batch.PERSISTENT)
+    plan.launch()
+    q, m, f = plan.result()
+    bufs = [(np.zeros(q * 8, np.uint32), np.zeros(q * 6, np.uint16), np.zeros(m * 12, np.uint32),
+             np.zeros(n * 5, np.uint32)) for _ in range(2)]
+    lib = rw.pool.lib
+    ctx.check(lib.hc_batch_plan_download(plan.handle, q, m, *(b.ctypes.data for b in bufs[0])), "download")
+    st = torch.cuda.Stream()
+    ctx.check(lib.hc_batch_plan_download_async(plan.handle, q, m, *(b.ctypes.data for b in bufs[1]), st.cuda_stream),
+              "download_async")
+    st.synchronize()
+    assert all(np.array_equal(a, b) for a, b in zip(*bufs))
+
+
 def test_batch_matches_single_chunk_call(ctx):
     from hypercraft_gb300 import batch
     w = _small_world("mixture")
