@@ -27,6 +27,7 @@ sys.path.insert(0, REPO)
 PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 DESC_BYTES = 48
+E2E_SETS = 3  # pools and plans in flight in the end-to-end measurement
 RESULT_BYTES = 20
 
 
@@ -339,9 +340,9 @@ def ours(args):
 
     # end to end through the C ABI with host buffers: every step uploads the world from pinned
     # memory, meshes it and reads every quad, mesh descriptor and per-chunk result back to pinned
-    # memory. Two pools and plans take the steps in turn on two streams, so one step's upload and
-    # download overlap the other's meshing (hc_batch_plan_download_async); the serial form (one
-    # step at a time, each waited for) is reported beside it.
+    # memory. E2E_SETS pools and plans take the steps in turn on their own streams, so a step's
+    # upload and download overlap the others' meshing (hc_batch_plan_download_async); the serial
+    # form (one step at a time, each waited for) is reported beside it.
     e2e = None
     if not args.no_e2e:
         hb = torch.from_numpy(w.blocks.view(np.int16)).pin_memory()
@@ -354,14 +355,16 @@ def ours(args):
                     torch.empty(meshes * 12, dtype=torch.int32).pin_memory(),
                     torch.empty(n * 5, dtype=torch.int32).pin_memory())
 
-        pool2 = batch.Pool(ctx, w.n_chunks)
-        arena2 = batch.Arena(arena.quad_capacity, arena.mesh_capacity, n, local)
-        plan2 = batch.BatchPlan(ctx, pool2, rw.neighbours, arena2, batch.variant_mode(variant))
-        stream2 = torch.cuda.Stream(device=dev)
-        sets = [(rw.pool, plan, sp, outputs()), (pool2, plan2, ctypes_stream(stream2), outputs())]
+        extra = []  # the other pools, arenas, plans and streams in flight
+        for _ in range(E2E_SETS - 1):
+            pool_x = batch.Pool(ctx, w.n_chunks)
+            arena_x = batch.Arena(arena.quad_capacity, arena.mesh_capacity, n, local)
+            plan_x = batch.BatchPlan(ctx, pool_x, rw.neighbours, arena_x, batch.variant_mode(variant))
+            extra.append((pool_x, arena_x, plan_x, torch.cuda.Stream(device=dev)))
+        sets = [(rw.pool, plan, sp, outputs())] + [(px, plx, ctypes_stream(stx), outputs()) for px, _, plx, stx in extra]
 
         def issue(k):
-            pool_k, plan_k, st_k, (ov, oi, od, orr) = sets[k % 2]
+            pool_k, plan_k, st_k, (ov, oi, od, orr) = sets[k % len(sets)]
             ctx.check(lib.hc_pool_upload(pool_k.handle, 0, w.n_chunks, hb.data_ptr(), hh.data_ptr(), 0, st_k), "upload")
             plan_k.launch(st_k)
             ctx.check(lib.hc_batch_plan_download_async(plan_k.handle, quads, meshes, ov.data_ptr(), oi.data_ptr(),
@@ -391,17 +394,19 @@ def ours(args):
         # both sets produced the whole output: the same per-chunk counts (arena placement may differ)
         for _, plan_k, _, _ in sets:
             assert plan_k.result() == (quads, meshes, 0)
-        r0, r1 = (x[3][3].view(-1, 5)[:, [0, 1, 3, 4]] for x in sets)
-        assert torch.equal(r0, r1), "the two pipelined sets differ"
+        r0 = sets[0][3][3].view(-1, 5)[:, [0, 1, 3, 4]]
+        assert all(torch.equal(r0, x[3][3].view(-1, 5)[:, [0, 1, 3, 4]]) for x in sets[1:]), "pipelined sets differ"
         t_serial = timed(lambda k: serial_step(), args.steps)
         e2e = {"value": chunks_all / t_pipe, "unit": "chunks/s",
                "h2d_bytes_per_step": int(w.n_chunks * (65536 + 1024)),
                "d2h_bytes_per_step": int(quads * 44 + meshes * DESC_BYTES + n * RESULT_BYTES),
-               "form": "two pools and plans in flight on two streams: a step's copies overlap the other's meshing",
+               "form": f"{E2E_SETS} pools and plans in flight on {E2E_SETS} streams: a step's copies overlap "
+                       "the others' meshing",
                "serial_value": chunks_all / t_serial}
-        plan2.close()
-        pool2.close()
-        del arena2
+        for pool_x, arena_x, plan_x, _ in extra:
+            plan_x.close()
+            pool_x.close()
+        del extra
 
     serving = None
     if rank == 0 and world == 1 and args.serve_seconds > 0:
