@@ -102,28 +102,27 @@ __device__ __forceinline__ void aabb_add(Smem &S, int st, uint32_t m, const uint
 	atomicMax(bb + 3, mx[0]), atomicMax(bb + 4, mx[1]), atomicMax(bb + 5, mx[2]);
 }
 
-// The same for the quads of a whole warp (all lanes call it; `valid` lanes carry a quad): the quads
-// of the first valid lane's mesh are reduced over the full warp first, so a mesh's box takes six
-// atomics per warp instead of six per quad; lanes of another mesh add theirs one by one.
+// The same for the quads of a whole warp (all lanes call it; `valid` lanes carry a quad): each mesh
+// among the warp's quads is reduced over the full warp in turn, so a mesh's box takes six atomics
+// per warp instead of six per quad.
 __device__ __forceinline__ void aabb_add_warp(Smem &S, bool valid, int st, uint32_t m, const uint32_t mn[3],
                                               const uint32_t mx[3]) {
-	const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
-	if (!vmask)
-		return;
-	const int leader = __ffs(vmask) - 1;
 	const uint32_t key = ((uint32_t)st << 16) | m;
-	const uint32_t lkey = __shfl_sync(0xffffffffu, key, leader);
-	const bool same = valid && key == lkey;
-	uint32_t r[6];
+	// one round per distinct mesh among the warp's quads (usually one or two: the two streams)
+	for (uint32_t pending = __ballot_sync(0xffffffffu, valid); pending;) {
+		const int leader = __ffs(pending) - 1;
+		const uint32_t lkey = __shfl_sync(0xffffffffu, key, leader);
+		const bool same = ((pending >> (threadIdx.x & 31)) & 1u) && key == lkey;
+		uint32_t r[6];
 #pragma unroll
-	for (int c = 0; c < 3; ++c) {
-		r[c] = __reduce_min_sync(0xffffffffu, same ? mn[c] : 0xffffffffu);
-		r[3 + c] = __reduce_max_sync(0xffffffffu, same ? mx[c] : 0u);
+		for (int c = 0; c < 3; ++c) {
+			r[c] = __reduce_min_sync(0xffffffffu, same ? mn[c] : 0xffffffffu);
+			r[3 + c] = __reduce_max_sync(0xffffffffu, same ? mx[c] : 0u);
+		}
+		if ((int)(threadIdx.x & 31) == leader)
+			aabb_add(S, (int)(lkey >> 16), lkey & 0xffffu, r, r + 3);
+		pending &= ~__ballot_sync(0xffffffffu, same);
 	}
-	if ((int)(threadIdx.x & 31) == leader)
-		aabb_add(S, (int)(lkey >> 16), lkey & 0xffffu, r, r + 3);
-	if (valid && !same)
-		aabb_add(S, st, m, mn, mx);
 }
 
 // Writes quad k of stream st (all-stream index g): 4 vertices, 6 indices, and the trigger of the
@@ -161,6 +160,7 @@ __device__ __forceinline__ void put_quad(Smem &S, const Emit &E, int st, uint32_
 __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	constexpr int kRows = kCls * kCls, kBatch = 12; // 1156 rows; 12 in flight per warp
+	constexpr int kApronRows = kRows - kChunk * kChunk; // 132
 	const uint8_t *own = reinterpret_cast<const uint8_t *>(&S.u);
 	if (S.pln[26]) {
 		// The blank test first, from the layer summaries of the chunk and its six face neighbours
@@ -185,12 +185,23 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 		has_custom = s_custom != 0;
 		if (s_blank)
 			return true;
-		// The chunk's own 32 KB of class ids are copied into the plane-mask scratch (unused until the
-		// light and plane passes) by asynchronous 16-byte copies, all in flight at once.
+		// The chunk's own 32 KB of class ids and the 132 x-rows of the apron (y or z outside [0, 32),
+		// x in [0, 32), 32 bytes each from a neighbour's planes) are copied into the plane-mask
+		// scratch (unused until the light and plane passes) by asynchronous 16-byte copies, all in
+		// flight at once.
 		const char *src = reinterpret_cast<const char *>(S.pln[26] + kPlaneClassOff);
 		const uint32_t dst = (uint32_t)__cvta_generic_to_shared(own);
 		for (int i = threadIdx.x; i < 32768 / 16; i += kThreads)
 			asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16 * i), "l"(src + 16 * i) : "memory");
+		for (int i = threadIdx.x; i < 2 * kApronRows; i += kThreads) {
+			const int a = i >> 1, half = i & 1;
+			const int y = a < 34 ? -1 : (a < 68 ? kChunk : (a - 68) >> 1);
+			const int z = a < 34 ? a - 1 : (a < 68 ? a - 35 : (((a - 68) & 1) ? kChunk : -1));
+			const char *row = reinterpret_cast<const char *>(S.pln[nb_index(0, y, z)] + kPlaneClassOff) +
+			                  ((y & 31) * kChunk + (z & 31)) * kChunk + 16 * half;
+			asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 32768 + 32 * a + 16 * half), "l"(row)
+			             : "memory");
+		}
 		asm volatile("cp.async.commit_group;" ::: "memory");
 		for (int i = threadIdx.x; i < 256; i += kThreads)
 			S.classes[i] = T.classes[i];
@@ -211,15 +222,16 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 		}
 		asm volatile("cp.async.wait_group 0;" ::: "memory");
 		__syncthreads();
-		// class ids of the cells x in [0, 32) of every row: the chunk's own from the copy, the
-		// apron's from the neighbours' planes; one warp per row, lanes over x
+		// class ids of the cells x in [0, 32) of every row, from the copies; one warp per row, lanes
+		// over x
 		for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
 			uint8_t c[kBatch];
 #pragma unroll
 			for (int j = 0; j < kBatch; ++j) {
 				const int row = min(row0 + j, kRows - 1), y = row / kCls - 1, z = row % kCls - 1;
 				const bool inner = (unsigned)y < (unsigned)kChunk && (unsigned)z < (unsigned)kChunk;
-				c[j] = inner ? own[lane + (y * kChunk + z) * kChunk] : class_byte(S, lane, y, z);
+				const int a = y < 0 ? z + 1 : (y >= kChunk ? 35 + z : 68 + 2 * y + (z >= kChunk)); // apron row
+				c[j] = own[inner ? lane + (y * kChunk + z) * kChunk : 32768 + 32 * a + lane];
 			}
 #pragma unroll
 			for (int j = 0; j < kBatch; ++j) {
