@@ -102,27 +102,28 @@ __device__ __forceinline__ void aabb_add(Smem &S, int st, uint32_t m, const uint
 	atomicMax(bb + 3, mx[0]), atomicMax(bb + 4, mx[1]), atomicMax(bb + 5, mx[2]);
 }
 
-// The same for the quads of a whole warp (all lanes call it; `valid` lanes carry a quad): each mesh
-// among the warp's quads is reduced over the full warp in turn, so a mesh's box takes six atomics
-// per warp instead of six per quad.
+// The same for the quads of a whole warp (all lanes call it; `valid` lanes carry a quad): the quads
+// of the first valid lane's mesh are reduced over the full warp first, so a mesh's box takes six
+// atomics per warp instead of six per quad; lanes of another mesh add theirs one by one.
 __device__ __forceinline__ void aabb_add_warp(Smem &S, bool valid, int st, uint32_t m, const uint32_t mn[3],
                                               const uint32_t mx[3]) {
+	const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+	if (!vmask)
+		return;
+	const int leader = __ffs(vmask) - 1;
 	const uint32_t key = ((uint32_t)st << 16) | m;
-	// one round per distinct mesh among the warp's quads (usually one or two: the two streams)
-	for (uint32_t pending = __ballot_sync(0xffffffffu, valid); pending;) {
-		const int leader = __ffs(pending) - 1;
-		const uint32_t lkey = __shfl_sync(0xffffffffu, key, leader);
-		const bool same = ((pending >> (threadIdx.x & 31)) & 1u) && key == lkey;
-		uint32_t r[6];
+	const uint32_t lkey = __shfl_sync(0xffffffffu, key, leader);
+	const bool same = valid && key == lkey;
+	uint32_t r[6];
 #pragma unroll
-		for (int c = 0; c < 3; ++c) {
-			r[c] = __reduce_min_sync(0xffffffffu, same ? mn[c] : 0xffffffffu);
-			r[3 + c] = __reduce_max_sync(0xffffffffu, same ? mx[c] : 0u);
-		}
-		if ((int)(threadIdx.x & 31) == leader)
-			aabb_add(S, (int)(lkey >> 16), lkey & 0xffffu, r, r + 3);
-		pending &= ~__ballot_sync(0xffffffffu, same);
+	for (int c = 0; c < 3; ++c) {
+		r[c] = __reduce_min_sync(0xffffffffu, same ? mn[c] : 0xffffffffu);
+		r[3 + c] = __reduce_max_sync(0xffffffffu, same ? mx[c] : 0u);
 	}
+	if ((int)(threadIdx.x & 31) == leader)
+		aabb_add(S, (int)(lkey >> 16), lkey & 0xffffu, r, r + 3);
+	if (valid && !same)
+		aabb_add(S, st, m, mn, mx);
 }
 
 // Writes quad k of stream st (all-stream index g): 4 vertices, 6 indices, and the trigger of the
