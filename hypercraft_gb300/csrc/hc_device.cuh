@@ -130,6 +130,7 @@ struct Smem {
 	const uint32_t *pln[27]; // per-chunk bit planes, or null (then the window is seeded from blocks)
 	const uint32_t *lvl[27]; // per-chunk level planes of the batch light pass, or null (then relight the window)
 	const uint32_t *edg[27]; // ... and their x = 0 / x = 31 edge bits
+	uint32_t lfl[27][2];     // ... and their uniform-plane bits per channel (LightPass::flags)
 	alignas(16) uint16_t cell[kClsCells + 8]; // per cell of [-1, 32]^3: light (low byte), class id (high byte)
 	union {
 		Relight rl;

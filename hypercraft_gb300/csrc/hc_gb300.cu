@@ -121,7 +121,8 @@ enum : uint32_t { kChunkBadSlot = 2 };
 // bits, found through the batch's own chunk numbering nbr_local.
 __device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes,
                           uint32_t pool_cap, const int32_t *nbr, uint32_t item, const uint32_t *levels = nullptr,
-                          const uint32_t *edges = nullptr, const int32_t *nbr_local = nullptr) {
+                          const uint32_t *edges = nullptr, const int32_t *nbr_local = nullptr,
+                          const uint32_t *lflags = nullptr) {
 	__shared__ int s_bad;
 	if (threadIdx.x == 0)
 		s_bad = 0;
@@ -141,6 +142,8 @@ __device__ bool load_refs(Smem &S, const uint16_t *pool_blocks, const int8_t *po
 			const size_t loc = levels ? (size_t)nbr_local[(size_t)item * 27 + threadIdx.x] : 0;
 			S.lvl[threadIdx.x] = levels ? levels + loc * kLevelSlotWords : nullptr;
 			S.edg[threadIdx.x] = levels ? edges + loc * kEdgeSlotWords : nullptr;
+			S.lfl[threadIdx.x][0] = lflags ? __ldg(lflags + 2 * loc) : 0u;
+			S.lfl[threadIdx.x][1] = lflags ? __ldg(lflags + 2 * loc + 1) : 0u;
 		}
 	}
 	__syncthreads();
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_mesh_batch(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
                  const int32_t *nbr, uint32_t n, const uint32_t *n_dev, unsigned int *work, unsigned int *failed,
                  DevTables T, Arena A, const uint32_t *levels, const uint32_t *edges, const int32_t *nbr_local,
-                 const uint8_t *item_blank) {
+                 const uint32_t *lflags, const uint8_t *item_blank) {
 	Smem &S = smem();
 	__shared__ uint32_t s_next;
 	if (n_dev) // the batch length is known on the device only (a world remesh)
@@ -220,7 +223,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 		if (item_blank && item_blank[item]) { // no quad: the results a blank chunk gets
 			if (threadIdx.x < 5)
 				A.results[5 * (size_t)item + threadIdx.x] = threadIdx.x == 4 ? kChunkOk : 0u;
-		} else if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, levels, edges, nbr_local)) {
+		} else if (load_refs(S, pool_blocks, pool_heights, pool_planes, pool_cap, nbr, item, levels, edges, nbr_local,
+		                     lflags)) {
 			mesh_chunk_cta(S, T, A, item);
 			if (threadIdx.x == 0 && A.results[5 * (size_t)item + 4] != kChunkOk)
 				atomicAdd(failed, 1u);
@@ -362,6 +366,7 @@ struct hc_batch_plan {
 	uint8_t *d_blank = nullptr;     // per chunk to mesh: blank (no quad), from the layer summaries
 	uint32_t *d_levels = nullptr;   // per batch chunk: 2 channels x 15 level planes
 	uint32_t *d_edges = nullptr;    // per batch chunk: their x = 0 and x = 31 bits
+	uint32_t *d_lflags = nullptr;   // per batch chunk and channel: which level planes are uniform
 	unsigned long long *d_state = nullptr; // quad cursor, mesh cursor, work counter, failed chunks
 	unsigned long long *h_state = nullptr; // pinned
 	uint2 *d_spill = nullptr;              // quad records past the shared buffer, per CTA of any grid
@@ -932,6 +937,8 @@ cudaError_t plan_light_tables(hc_batch_plan *p, const std::vector<int32_t> &tabl
 		e = cudaMalloc(&p->d_levels, (size_t)m * kLevelSlotWords * sizeof(uint32_t));
 	if (e == cudaSuccess)
 		e = cudaMalloc(&p->d_edges, (size_t)m * kEdgeSlotWords * sizeof(uint32_t));
+	if (e == cudaSuccess)
+		e = cudaMalloc(&p->d_lflags, (size_t)m * 2 * sizeof(uint32_t));
 	return e;
 }
 
@@ -971,7 +978,8 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		return s;
 	const bool light_pass = p->variant == HC_VARIANT_LIGHT_PASS && p->d_levels;
 	if (light_pass) {
-		const LightPass L{p->d_slots, p->d_nb6, p->pool->d_planes, p->pool->d_blocks, p->d_levels, p->d_edges, p->n_slots};
+		const LightPass L{p->d_slots,  p->d_nb6,   p->pool->d_planes, p->pool->d_blocks,
+		                  p->d_levels, p->d_edges, p->d_lflags,       p->n_slots};
 		for (int t = kLevels; t >= 1; --t) {
 			k_light_level<<<p->n_slots, kLightThreads, 0, st>>>(L, tables(ctx), t);
 			HC_CUDA(ctx, cudaGetLastError());
@@ -995,7 +1003,7 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(
 		    p->pool->d_blocks, p->pool->d_heights, p->pool->d_planes, p->pool->capacity, p->nbr, p->n, nullptr, work,
 		    failed, tables(ctx), A, light_pass ? p->d_levels : nullptr, light_pass ? p->d_edges : nullptr,
-		    light_pass ? p->d_nbr_local : nullptr, p->d_blank);
+		    light_pass ? p->d_nbr_local : nullptr, light_pass ? p->d_lflags : nullptr, p->d_blank);
 		HC_CUDA(ctx, cudaGetLastError());
 	} else {
 		for (uint32_t i = 0; i < p->n; ++i) {
@@ -1188,6 +1196,7 @@ void hc_batch_plan_destroy(hc_batch_plan *plan) {
 	cudaFree(plan->d_nbr_local);
 	cudaFree(plan->d_levels);
 	cudaFree(plan->d_edges);
+	cudaFree(plan->d_lflags);
 	cudaFree(plan->d_state);
 	cudaFree(plan->d_spill);
 	cudaFree(plan->d_blank);
@@ -1385,7 +1394,7 @@ hc_status world_enqueue_remesh(hc_world *w, const hc_batch_arena *arena, cudaStr
 	} else {
 		k_mesh_batch<<<w->sms, kThreads, ctx->smem_bytes, st>>>(
 		    w->pool->d_blocks, w->pool->d_heights, w->pool->d_planes, w->pool->capacity, w->d_nbr, 0u,
-		    w->d_counts + kCountRemesh, work, failed, tables(ctx), A, nullptr, nullptr, nullptr, nullptr);
+		    w->d_counts + kCountRemesh, work, failed, tables(ctx), A, nullptr, nullptr, nullptr, nullptr, nullptr);
 	}
 	HC_CUDA(ctx, cudaGetLastError());
 	k_requeue<<<list_grid(w), 256, 0, st>>>(W, w->d_list, A.results);
@@ -1920,7 +1929,7 @@ extern "C" hc_status hc_mesh_batch_noalloc(const uint16_t *pool_blocks, const in
 		        results};
 		k_mesh_batch<<<D.sms, kThreads, sizeof(Smem), st>>>(pool_blocks, pool_heights, nullptr, pool_capacity, neighbours,
 		                                                     n, nullptr, state + 4, state + 5, DevTables{D.class_of, D.classes}, A,
-		                                                     nullptr, nullptr, nullptr, nullptr);
+		                                                     nullptr, nullptr, nullptr, nullptr, nullptr);
 		e = cudaGetLastError();
 	}
 	uint32_t host_state[kNoAllocStateWords];

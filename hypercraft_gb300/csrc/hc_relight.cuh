@@ -405,8 +405,22 @@ struct LightPass {
 	const uint16_t *blocks; // pool blocks (rows with emitters below 15)
 	uint32_t *levels;       // batch chunk -> channel -> level t at plane t - 1 -> 1024 rows
 	uint32_t *edges;        // batch chunk -> channel -> level -> {bit x = 0, bit x = 31} of every row
+	uint32_t *flags;        // batch chunk -> channel -> kFlag* bits of its level planes
 	uint32_t n;             // batch chunks
 };
+
+// Per batch chunk and channel, which level planes are uniform: bit t - 1 = level t is empty, bit
+// 16 + t - 1 = level t is full. A uniform plane below level 15 whose value follows from level t + 1
+// (full stays full; empty stays empty when the six face neighbours are empty and no emitter seeds
+// it) is neither computed nor stored: every reader takes its value from these bits. Bit 15 of the
+// torch word: the chunk holds emitters below level 15.
+enum : uint32_t { kFlagFull = 16, kFlagLowEmitters = 1u << 15 };
+__device__ __forceinline__ bool level_empty(uint32_t f, int t) { return (f >> (t - 1)) & 1u; }
+__device__ __forceinline__ bool level_full(uint32_t f, int t) { return (f >> (kFlagFull + t - 1)) & 1u; }
+// The word of a level plane row (or edge word) from its chunk's flags, or loaded when not uniform.
+__device__ __forceinline__ uint32_t level_word(uint32_t f, int t, const uint32_t *p) {
+	return level_empty(f, t) ? 0u : (level_full(f, t) ? 0xffffffffu : __ldg(p));
+}
 
 __device__ __forceinline__ const uint32_t *level_plane(const LightPass &L, int i, int c, int t) {
 	return L.levels + (size_t)i * kLevelSlotWords + (size_t)(c * kLevels + t - 1) * kPlaneWords;
@@ -430,53 +444,135 @@ __device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
 // edge bits of its six face neighbours that touch it are staged in shared memory with coalesced
 // loads (the chunk's own rows are requested before its neighbour list arrives), then each thread
 // dilates kLightRows rows of both channels. Also writes the row edge bits that the x neighbours
-// read at the next level.
+// read at the next level, and the plane's uniform bits (LightPass::flags). A channel whose level
+// follows from level t + 1 without computing (see kFlag*) is skipped: a chunk of sunlit air far
+// from any emitter costs one flag word per level.
 __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevTables T, int t) {
 	__shared__ __align__(16) uint32_t prev[2][kPlaneWords];
 	__shared__ uint32_t side[2][6][32]; // per channel: -x hi edge, +x lo edge, -y rows, +y rows, -z rows, +z rows
 	__shared__ int s_nb[6];
 	__shared__ int32_t s_slot;
+	__shared__ uint32_t s_fl[7][2]; // level t + 1 flags: the six face neighbours, then the chunk
+	__shared__ uint32_t s_run;      // bit c: channel c is computed at this level
 	const int tid = threadIdx.x, lane = tid & 31;
 	const int i = blockIdx.x;
-	constexpr int kQ = 2 * kPlaneWords / 4 / kLightThreads; // uint4 of the two channels per thread
-	uint4 own[kQ];
-	if (t < kLevels) {
+	if (t == kLevels) { // the seeds: sunlit cells, emitters of level 15; every plane is stored
+		if (tid == 0)
+			s_slot = __ldg(L.slots + i);
+		__syncthreads();
+		const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
+		uint32_t s[kLightRows][2];
+		bool any[2] = {false, false}, all[2] = {true, true}, low = false;
 #pragma unroll
-		for (int q = 0; q < kQ; ++q) {
-			const int j = tid + q * kLightThreads, c = j / (kPlaneWords / 4), o = j % (kPlaneWords / 4);
-			own[q] = __ldg(reinterpret_cast<const uint4 *>(level_plane(L, i, c, t + 1)) + o);
+		for (int k = 0; k < kLightRows; ++k) {
+			const int r = tid + k * kLightThreads;
+			s[k][0] = __ldg(P + kPlaneSun * kPlaneWords + r);
+			s[k][1] = __ldg(P + kPlaneT15 * kPlaneWords + r);
+			low |= ((__ldg(P + kPlaneLowOff + (r >> 5)) >> (r & 31)) & 1u) != 0;
+#pragma unroll
+			for (int c = 0; c < 2; ++c)
+				any[c] |= s[k][c] != 0, all[c] &= s[k][c] == 0xffffffffu;
 		}
+		uint32_t fl[2];
+#pragma unroll
+		for (int c = 0; c < 2; ++c) {
+			const bool a = __syncthreads_or(any[c]), f = __syncthreads_and(all[c]);
+			fl[c] = (a ? 0u : 1u << (kLevels - 1)) | (f ? 1u << (kFlagFull + kLevels - 1) : 0u);
+		}
+		fl[1] |= __syncthreads_or(low) ? kFlagLowEmitters : 0u;
+#pragma unroll
+		for (int k = 0; k < kLightRows; ++k) {
+			const int r = tid + k * kLightThreads;
+#pragma unroll
+			for (int c = 0; c < 2; ++c) {
+				L.levels[(size_t)i * kLevelSlotWords + (size_t)(c * kLevels + kLevels - 1) * kPlaneWords + r] = s[k][c];
+				const uint32_t lo = __ballot_sync(0xffffffffu, s[k][c] & 1u), hi = __ballot_sync(0xffffffffu, s[k][c] >> 31);
+				if (lane == 0) {
+					uint32_t *e = L.edges + (size_t)i * kEdgeSlotWords + (size_t)(c * kLevels + kLevels - 1) * 64;
+					e[r >> 5] = lo;
+					e[32 + (r >> 5)] = hi;
+				}
+			}
+		}
+		if (tid < 2)
+			L.flags[2 * (size_t)i + tid] = fl[tid];
+		return;
 	}
 	if (tid < 6)
 		s_nb[tid] = __ldg(L.nb6 + 6 * i + tid);
 	if (tid == 6)
 		s_slot = __ldg(L.slots + i);
+	if (tid < 2)
+		s_fl[6][tid] = __ldg(L.flags + 2 * (size_t)i + tid);
 	__syncthreads();
-	const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
-	if (t < kLevels) {
-		for (int j = tid; j < 2 * 6 * 32; j += kLightThreads) {
-			const int c = j / 192, f = (j / 32) % 6, k = j & 31, nb = s_nb[f];
-			uint32_t v = 0;
-			if (nb >= 0) {
-				if (f == 0)
-					v = __ldg(level_edges(L, nb, c, t + 1) + 32 + k); // x = 31 bits of the -x neighbour
-				else if (f == 1)
-					v = __ldg(level_edges(L, nb, c, t + 1) + k); // x = 0 bits of the +x neighbour
-				else if (f == 2)
-					v = __ldg(level_plane(L, nb, c, t + 1) + 31 * 32 + k); // its y = 31 row at z = k
-				else if (f == 3)
-					v = __ldg(level_plane(L, nb, c, t + 1) + k); // y = 0, z = k
-				else if (f == 4)
-					v = __ldg(level_plane(L, nb, c, t + 1) + k * 32 + 31); // z = 31 row at y = k
-				else
-					v = __ldg(level_plane(L, nb, c, t + 1) + k * 32); // z = 0, y = k
+	if (tid < 12) { // the neighbours' flags (a missing neighbour is dark: empty)
+		const int f = tid >> 1, c = tid & 1, nb = s_nb[f];
+		s_fl[f][c] = nb >= 0 ? __ldg(L.flags + 2 * (size_t)nb + c) : 0xffffu;
+	}
+	__syncthreads();
+	if (tid == 0) {
+		uint32_t run = 0;
+#pragma unroll
+		for (int c = 0; c < 2; ++c) {
+			const uint32_t own = s_fl[6][c];
+			bool trivial = level_full(own, t + 1);
+			if (!trivial && level_empty(own, t + 1) && !(c == 1 && (own & kFlagLowEmitters))) {
+				trivial = true;
+				for (int f = 0; f < 6; ++f)
+					trivial &= level_empty(s_fl[f][c], t + 1);
 			}
-			side[c][f][k] = v;
+			uint32_t bits = 0;
+			if (trivial) // the level follows: full stays full, empty stays empty
+				bits = level_full(own, t + 1) ? 1u << (kFlagFull + t - 1) : 1u << (t - 1);
+			else
+				run |= 1u << c;
+			if (bits)
+				atomicOr(L.flags + 2 * (size_t)i + c, bits);
 		}
+		s_run = run;
+	}
+	__syncthreads();
+	const uint32_t run = s_run;
+	if (!run)
+		return;
+	const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
+	constexpr int kQ = kPlaneWords / 4 / kLightThreads; // uint4 of one channel per thread
+#pragma unroll
+	for (int c = 0; c < 2; ++c) {
+		if (!((run >> c) & 1u))
+			continue;
+		const uint32_t own = s_fl[6][c];
 #pragma unroll
 		for (int q = 0; q < kQ; ++q) {
-			const int j = tid + q * kLightThreads, c = j / (kPlaneWords / 4), o = j % (kPlaneWords / 4);
-			reinterpret_cast<uint4 *>(prev[c])[o] = own[q];
+			const int o = tid + q * kLightThreads;
+			uint4 v;
+			if (level_empty(own, t + 1))
+				v = make_uint4(0u, 0u, 0u, 0u);
+			else if (level_full(own, t + 1))
+				v = make_uint4(~0u, ~0u, ~0u, ~0u);
+			else
+				v = __ldg(reinterpret_cast<const uint4 *>(level_plane(L, i, c, t + 1)) + o);
+			reinterpret_cast<uint4 *>(prev[c])[o] = v;
+		}
+		for (int j = tid; j < 6 * 32; j += kLightThreads) {
+			const int f = j >> 5, k = j & 31, nb = s_nb[f];
+			uint32_t v = 0;
+			if (nb >= 0) {
+				const uint32_t fl = s_fl[f][c];
+				if (f == 0)
+					v = level_word(fl, t + 1, level_edges(L, nb, c, t + 1) + 32 + k); // x = 31 bits of the -x neighbour
+				else if (f == 1)
+					v = level_word(fl, t + 1, level_edges(L, nb, c, t + 1) + k); // x = 0 bits of the +x neighbour
+				else if (f == 2)
+					v = level_word(fl, t + 1, level_plane(L, nb, c, t + 1) + 31 * 32 + k); // its y = 31 row at z = k
+				else if (f == 3)
+					v = level_word(fl, t + 1, level_plane(L, nb, c, t + 1) + k); // y = 0, z = k
+				else if (f == 4)
+					v = level_word(fl, t + 1, level_plane(L, nb, c, t + 1) + k * 32 + 31); // z = 31 row at y = k
+				else
+					v = level_word(fl, t + 1, level_plane(L, nb, c, t + 1) + k * 32); // z = 0, y = k
+			}
+			side[c][f][k] = v;
 		}
 	}
 	uint32_t pass[kLightRows], lows[kLightRows], s[kLightRows][2];
@@ -484,34 +580,27 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 	for (int k = 0; k < kLightRows; ++k) {
 		const int r = tid + k * kLightThreads;
 		pass[k] = __ldg(P + kPlanePass * kPlaneWords + r);
-		lows[k] = __ldg(P + kPlaneLowOff + (r >> 5));
-		if (t == kLevels) {
-			s[k][0] = __ldg(P + kPlaneSun * kPlaneWords + r);
-			s[k][1] = __ldg(P + kPlaneT15 * kPlaneWords + r);
-		}
+		lows[k] = (run & 2u) ? __ldg(P + kPlaneLowOff + (r >> 5)) : 0u;
 	}
 	__syncthreads();
-	if (t < kLevels) {
-#pragma unroll
-		for (int k = 0; k < kLightRows; ++k) {
-			const int r = tid + k * kLightThreads, y = r >> 5, z = r & 31;
-#pragma unroll
-			for (int c = 0; c < 2; ++c) {
-				const uint32_t me = prev[c][r];
-				uint32_t d = (me << 1) | (me >> 1);
-				d |= (side[c][0][r >> 5] >> (r & 31)) & 1u;
-				d |= ((side[c][1][r >> 5] >> (r & 31)) & 1u) << 31;
-				d |= y > 0 ? prev[c][r - 32] : side[c][2][z];
-				d |= y < 31 ? prev[c][r + 32] : side[c][3][z];
-				d |= z > 0 ? prev[c][r - 1] : side[c][4][y];
-				d |= z < 31 ? prev[c][r + 1] : side[c][5][y];
-				s[k][c] = me | (pass[k] & d);
-			}
-		}
-	}
+	bool any[2] = {false, false}, all[2] = {true, true};
 #pragma unroll
 	for (int k = 0; k < kLightRows; ++k) {
-		const int r = tid + k * kLightThreads;
+		const int r = tid + k * kLightThreads, y = r >> 5, z = r & 31;
+#pragma unroll
+		for (int c = 0; c < 2; ++c) {
+			if (!((run >> c) & 1u))
+				continue;
+			const uint32_t me = prev[c][r];
+			uint32_t d = (me << 1) | (me >> 1);
+			d |= (side[c][0][r >> 5] >> (r & 31)) & 1u;
+			d |= ((side[c][1][r >> 5] >> (r & 31)) & 1u) << 31;
+			d |= y > 0 ? prev[c][r - 32] : side[c][2][z];
+			d |= y < 31 ? prev[c][r + 32] : side[c][3][z];
+			d |= z > 0 ? prev[c][r - 1] : side[c][4][y];
+			d |= z < 31 ? prev[c][r + 1] : side[c][5][y];
+			s[k][c] = me | (pass[k] & d);
+		}
 		if ((lows[k] >> (r & 31)) & 1u) { // emitters below level 15 in this row
 			const uint16_t *row = L.blocks + (size_t)s_slot * 32768 + r * 32;
 			for (int x = 0; x < 32; ++x)
@@ -520,6 +609,9 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 		}
 #pragma unroll
 		for (int c = 0; c < 2; ++c) {
+			if (!((run >> c) & 1u))
+				continue;
+			any[c] |= s[k][c] != 0, all[c] &= s[k][c] == 0xffffffffu;
 			uint32_t *out = L.levels + (size_t)i * kLevelSlotWords + (size_t)(c * kLevels + t - 1) * kPlaneWords;
 			out[r] = s[k][c];
 			const uint32_t lo = __ballot_sync(0xffffffffu, s[k][c] & 1u), hi = __ballot_sync(0xffffffffu, s[k][c] >> 31);
@@ -529,6 +621,15 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 				e[32 + (r >> 5)] = hi;
 			}
 		}
+	}
+	// a computed plane that came out uniform is flagged too (it is stored as well)
+#pragma unroll
+	for (int c = 0; c < 2; ++c) {
+		if (!((run >> c) & 1u))
+			continue;
+		const bool a = __syncthreads_or(any[c]), f = __syncthreads_and(all[c]);
+		if (tid == 0 && (!a || f))
+			atomicOr(L.flags + 2 * (size_t)i + c, !a ? 1u << (t - 1) : 1u << (kFlagFull + t - 1));
 	}
 }
 
@@ -562,27 +663,30 @@ __device__ void light_from_levels(Smem &S) {
 	constexpr int kRowItems = kLt * kLt, kItems = kRowItems + 2 * kLt * 3;
 	for (int it = threadIdx.x; it < kItems; it += kThreads) {
 		const uint32_t *src;
-		int stride;
+		int stride, nb;
 		int x = 0, y, zc = 1, z0 = 0;
 		if (it < kRowItems) {
 			y = it / kLt - 1;
 			const int z = it % kLt - 1;
-			src = S.lvl[nb_index(0, y, z)] + (y & 31) * 32 + (z & 31);
+			nb = nb_index(0, y, z);
+			src = S.lvl[nb] + (y & 31) * 32 + (z & 31);
 			stride = kPlaneWords;
 		} else {
 			const int k = it - kRowItems, side = k / (kLt * 3), rem = k - side * (kLt * 3);
 			y = rem / 3 - 1, zc = rem % 3;
 			x = side ? kChunk : -1, z0 = zc == 0 ? -1 : (zc == 1 ? 0 : kChunk);
-			src = S.edg[nb_index(x, y, z0)] + (side ? 0 : 32) + (y & 31); // x = 0 or x = 31 bits over z
+			nb = nb_index(x, y, z0);
+			src = S.edg[nb] + (side ? 0 : 32) + (y & 31); // x = 0 or x = 31 bits over z
 			stride = 64;
 		}
 		uint32_t b[2][4];
 #pragma unroll
 		for (int c = 0; c < 2; ++c) {
+			const uint32_t fl = S.lfl[nb][c]; // uniform planes are not stored
 			uint32_t lv[kLevels];
 #pragma unroll
 			for (int u = 0; u < kLevels; ++u)
-				lv[u] = __ldg(src + (size_t)(c * kLevels + u) * stride);
+				lv[u] = level_word(fl, u + 1, src + (size_t)(c * kLevels + u) * stride);
 			level_bits(lv, b[c]);
 		}
 		const uint32_t w[8] = {b[0][0], b[0][1], b[0][2], b[0][3], b[1][0], b[1][1], b[1][2], b[1][3]};
