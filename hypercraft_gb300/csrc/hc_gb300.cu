@@ -937,8 +937,8 @@ cudaError_t plan_light_tables(hc_batch_plan *p, const std::vector<int32_t> &tabl
 		e = cudaMalloc(&p->d_levels, (size_t)m * kLevelSlotWords * sizeof(uint32_t));
 	if (e == cudaSuccess)
 		e = cudaMalloc(&p->d_edges, (size_t)m * kEdgeSlotWords * sizeof(uint32_t));
-	if (e == cudaSuccess)
-		e = cudaMalloc(&p->d_lflags, (size_t)m * 2 * sizeof(uint32_t));
+	if (e == cudaSuccess) // the uniform-plane flags, then the neighbour-light bits (LightPass::near)
+		e = cudaMalloc(&p->d_lflags, (size_t)m * 4 * sizeof(uint32_t));
 	return e;
 }
 
@@ -978,8 +978,9 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		return s;
 	const bool light_pass = p->variant == HC_VARIANT_LIGHT_PASS && p->d_levels;
 	if (light_pass) {
-		const LightPass L{p->d_slots,  p->d_nb6,   p->pool->d_planes, p->pool->d_blocks,
-		                  p->d_levels, p->d_edges, p->d_lflags,       p->n_slots};
+		const LightPass L{p->d_slots,  p->d_nb6,   p->pool->d_planes, p->pool->d_blocks, p->d_levels,
+		                  p->d_edges, p->d_lflags, p->d_lflags + 2 * (size_t)p->n_slots, p->n_slots};
+		HC_CUDA(ctx, cudaMemsetAsync(L.near, 0, 2 * (size_t)p->n_slots * sizeof(uint32_t), st));
 		for (int t = kLevels; t >= 1; --t) {
 			k_light_level<<<p->n_slots, kLightThreads, 0, st>>>(L, tables(ctx), t);
 			HC_CUDA(ctx, cudaGetLastError());

@@ -406,6 +406,8 @@ struct LightPass {
 	uint32_t *levels;       // batch chunk -> channel -> level t at plane t - 1 -> 1024 rows
 	uint32_t *edges;        // batch chunk -> channel -> level -> {bit x = 0, bit x = 31} of every row
 	uint32_t *flags;        // batch chunk -> channel -> kFlag* bits of its level planes
+	uint32_t *near;         // batch chunk -> channel -> bit t - 1: some face neighbour (or the chunk) has a
+	                        // non-empty level t + 1 (set by those chunks; cleared before the pass)
 	uint32_t n;             // batch chunks
 };
 
@@ -447,7 +449,7 @@ __device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
 // read at the next level, and the plane's uniform bits (LightPass::flags). A channel whose level
 // follows from level t + 1 without computing (see kFlag*) is skipped: a chunk of sunlit air far
 // from any emitter costs one flag word per level.
-__global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevTables T, int t) {
+__global__ void __launch_bounds__(kLightThreads, 8) k_light_level(LightPass L, DevTables T, int t) {
 	__shared__ __align__(16) uint32_t prev[2][kPlaneWords];
 	__shared__ uint32_t side[2][6][32]; // per channel: -x hi edge, +x lo edge, -y rows, +y rows, -z rows, +z rows
 	__shared__ int s_nb[6];
@@ -496,49 +498,60 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 		}
 		if (tid < 2)
 			L.flags[2 * (size_t)i + tid] = fl[tid];
+		if (tid < 14) { // a non-empty level 15 may light this chunk and its face neighbours at level 14
+			const int c = tid / 7, f = tid % 7;
+			const int nb = f < 6 ? __ldg(L.nb6 + 6 * i + f) : i;
+			if (nb >= 0 && !level_empty(fl[c], kLevels))
+				atomicOr(L.near + 2 * (size_t)nb + c, 1u << (kLevels - 2));
+		}
 		return;
 	}
+	__shared__ uint32_t s_near[2];
 	if (tid < 6)
 		s_nb[tid] = __ldg(L.nb6 + 6 * i + tid);
 	if (tid == 6)
 		s_slot = __ldg(L.slots + i);
-	if (tid < 2)
+	if (tid < 2) {
 		s_fl[6][tid] = __ldg(L.flags + 2 * (size_t)i + tid);
-	__syncthreads();
-	if (tid < 12) { // the neighbours' flags (a missing neighbour is dark: empty)
-		const int f = tid >> 1, c = tid & 1, nb = s_nb[f];
-		s_fl[f][c] = nb >= 0 ? __ldg(L.flags + 2 * (size_t)nb + c) : 0xffffu;
+		s_near[tid] = __ldg(L.near + 2 * (size_t)i + tid);
 	}
 	__syncthreads();
-	if (tid == 0) {
+	if (tid == 0) { // which channels follow from level t + 1 without computing
 		uint32_t run = 0;
 #pragma unroll
 		for (int c = 0; c < 2; ++c) {
 			const uint32_t own = s_fl[6][c];
-			bool trivial = level_full(own, t + 1);
-			if (!trivial && level_empty(own, t + 1) && !(c == 1 && (own & kFlagLowEmitters))) {
-				trivial = true;
-				for (int f = 0; f < 6; ++f)
-					trivial &= level_empty(s_fl[f][c], t + 1);
-			}
-			uint32_t bits = 0;
-			if (trivial) // the level follows: full stays full, empty stays empty
-				bits = level_full(own, t + 1) ? 1u << (kFlagFull + t - 1) : 1u << (t - 1);
+			// full stays full; empty stays empty when no face neighbour had light at level t + 1 and no
+			// emitter seeds level t
+			const bool full = level_full(own, t + 1);
+			const bool trivial = full || (level_empty(own, t + 1) && !((s_near[c] >> (t - 1)) & 1u) &&
+			                              !(c == 1 && (own & kFlagLowEmitters)));
+			if (trivial)
+				atomicOr(L.flags + 2 * (size_t)i + c, full ? 1u << (kFlagFull + t - 1) : 1u << (t - 1));
 			else
 				run |= 1u << c;
-			if (bits)
-				atomicOr(L.flags + 2 * (size_t)i + c, bits);
 		}
 		s_run = run;
 	}
 	__syncthreads();
 	const uint32_t run = s_run;
+	// a full plane at level t (it stays full) lights this chunk and its face neighbours at level t - 1
+	if (t > 1 && tid < 14) {
+		const int c = tid / 7, f = tid % 7;
+		const int nb = f < 6 ? s_nb[f] : i;
+		if (nb >= 0 && !((run >> c) & 1u) && level_full(s_fl[6][c], t + 1))
+			atomicOr(L.near + 2 * (size_t)nb + c, 1u << (t - 2));
+	}
 	if (!run)
 		return;
+	if (tid < 12) { // the neighbours' flags (a missing neighbour is dark: empty)
+		const int f = tid >> 1, c = tid & 1, nb = s_nb[f];
+		s_fl[f][c] = nb >= 0 ? __ldg(L.flags + 2 * (size_t)nb + c) : 0xffffu;
+	}
 	const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
 	constexpr int kQ = kPlaneWords / 4 / kLightThreads; // uint4 of one channel per thread
 #pragma unroll
-	for (int c = 0; c < 2; ++c) {
+	for (int c = 0; c < 2; ++c) { // the chunk's own level t + 1 rows, meanwhile
 		if (!((run >> c) & 1u))
 			continue;
 		const uint32_t own = s_fl[6][c];
@@ -554,6 +567,12 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 				v = __ldg(reinterpret_cast<const uint4 *>(level_plane(L, i, c, t + 1)) + o);
 			reinterpret_cast<uint4 *>(prev[c])[o] = v;
 		}
+	}
+	__syncthreads();
+#pragma unroll
+	for (int c = 0; c < 2; ++c) {
+		if (!((run >> c) & 1u))
+			continue;
 		for (int j = tid; j < 6 * 32; j += kLightThreads) {
 			const int f = j >> 5, k = j & 31, nb = s_nb[f];
 			uint32_t v = 0;
@@ -622,7 +641,8 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 			}
 		}
 	}
-	// a computed plane that came out uniform is flagged too (it is stored as well)
+	// a computed plane that came out uniform is flagged too (it is stored as well); a non-empty one
+	// lights this chunk and its face neighbours at level t - 1
 #pragma unroll
 	for (int c = 0; c < 2; ++c) {
 		if (!((run >> c) & 1u))
@@ -630,6 +650,11 @@ __global__ void __launch_bounds__(kLightThreads) k_light_level(LightPass L, DevT
 		const bool a = __syncthreads_or(any[c]), f = __syncthreads_and(all[c]);
 		if (tid == 0 && (!a || f))
 			atomicOr(L.flags + 2 * (size_t)i + c, !a ? 1u << (t - 1) : 1u << (kFlagFull + t - 1));
+		if (a && t > 1 && tid < 7) {
+			const int nb = tid < 6 ? s_nb[tid] : i;
+			if (nb >= 0)
+				atomicOr(L.near + 2 * (size_t)nb + c, 1u << (t - 2));
+		}
 	}
 }
 
