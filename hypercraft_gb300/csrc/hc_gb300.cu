@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mesh_single(Refs27 refs, DevTab
 }
 
 // Planes of the listed pool slots (grid-stride over slot x row).
-__global__ void __launch_bounds__(256) k_planes_pool(const uint16_t *pool_blocks, const int8_t *pool_heights,
+__global__ void __launch_bounds__(256, 4) k_planes_pool(const uint16_t *pool_blocks, const int8_t *pool_heights,
                                                       const int32_t *slots, uint32_t n, DevTables T, uint32_t *planes) {
 	__shared__ DevClass cls[256];
 	for (int i = threadIdx.x; i < 256; i += blockDim.x)

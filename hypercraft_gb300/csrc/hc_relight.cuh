@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(kLightThreads, 8) k_light_level(LightPass L, D
 	__shared__ uint32_t s_run;      // bit c: channel c is computed at this level
 	const int tid = threadIdx.x, lane = tid & 31;
 	const int i = blockIdx.x;
-	if (t == kLevels) { // the seeds: sunlit cells, emitters of level 15; every plane is stored
+	if (t == kLevels) { // the seeds: sunlit cells, emitters of level 15 (uniform planes are not stored)
 		if (tid == 0)
 			s_slot = __ldg(L.slots + i);
 		__syncthreads();
@@ -476,10 +476,12 @@ __global__ void __launch_bounds__(kLightThreads, 8) k_light_level(LightPass L, D
 				any[c] |= s[k][c] != 0, all[c] &= s[k][c] == 0xffffffffu;
 		}
 		uint32_t fl[2];
+		bool store[2];
 #pragma unroll
 		for (int c = 0; c < 2; ++c) {
 			const bool a = __syncthreads_or(any[c]), f = __syncthreads_and(all[c]);
 			fl[c] = (a ? 0u : 1u << (kLevels - 1)) | (f ? 1u << (kFlagFull + kLevels - 1) : 0u);
+			store[c] = a && !f;
 		}
 		fl[1] |= __syncthreads_or(low) ? kFlagLowEmitters : 0u;
 #pragma unroll
@@ -487,6 +489,8 @@ __global__ void __launch_bounds__(kLightThreads, 8) k_light_level(LightPass L, D
 			const int r = tid + k * kLightThreads;
 #pragma unroll
 			for (int c = 0; c < 2; ++c) {
+				if (!store[c])
+					continue;
 				L.levels[(size_t)i * kLevelSlotWords + (size_t)(c * kLevels + kLevels - 1) * kPlaneWords + r] = s[k][c];
 				const uint32_t lo = __ballot_sync(0xffffffffu, s[k][c] & 1u), hi = __ballot_sync(0xffffffffu, s[k][c] >> 31);
 				if (lane == 0) {
