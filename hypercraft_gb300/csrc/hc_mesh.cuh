@@ -663,15 +663,17 @@ __device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
 // For every row with quads the whole warp calls t = on_starts(starts) as soon as the row's quad
 // starts are known (so that what it starts, e.g. an atomic, overlaps the height search) and then
 // on_row(t, u, starts, tmask, is_start, w, h); the quad of lane v (is_start) is (u, v, w, h) and its
-// stream is bit v of tmask.
+// stream is bit v of tmask. Only the rows in `only` are scanned: a caller may leave out rows that
+// no quad of another row reaches and whose own quads do not grow down (see plane_count_one).
 template <typename G, typename F>
-__device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], G &&on_starts, F &&on_row) {
+__device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], G &&on_starts, F &&on_row,
+                                                 uint32_t only = 0xffffffffu) {
 	const int lane = threadIdx.x & 31;
 	const uint32_t rN = m[lane][0], rE = m[lane][1], rT = m[lane][3];
 	const uint32_t Dc = warp_transpose32(m[lane][2]); // bit r: cell (r, lane) equals cell (r + 1, lane)
 	const uint32_t upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
 	uint32_t Cc = 0;                                   // bit r: cell (r, lane) is covered
-	uint32_t rows = __ballot_sync(0xffffffffu, rN != 0);
+	uint32_t rows = __ballot_sync(0xffffffffu, rN != 0) & only;
 	while (rows) {
 		const int u = __ffs(rows) - 1;
 		rows &= rows - 1;
@@ -726,33 +728,91 @@ __device__ __forceinline__ uint2 get_record(const Smem &S, uint32_t j) {
 	return j < (uint32_t)kQuadBuf ? S.aux.quads[j] : S.spill[j - kQuadBuf];
 }
 
+// Warp exclusive prefix sum over lanes of a value packing two 16-bit counts; *total gets the sum.
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t x, uint32_t *total) {
+	const int lane = threadIdx.x & 31;
+	uint32_t incl = x;
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+		if (lane >= d)
+			incl += o;
+	}
+	*total = __shfl_sync(0xffffffffu, incl, 31);
+	return incl - x;
+}
+
 // Counts the quads of plane p (the calling warp) and keeps their records; misc[4] = records kept.
+// A row none of whose cells equals the one below, below a row of which the same holds, is
+// isolated: no quad of another row reaches it and its own quads do not grow down, so its quads are
+// its horizontal runs (height 1) and its rows above and below scan as if it were not there. Lane u
+// takes isolated row u, all at once; the exact row scan (warp_merge_plane) visits the other rows.
+// A quad's index among the plane's quads (u-major, then v; all streams and per stream) counts the
+// quads of the earlier rows of both kinds: isolated rows first give their per-row counts to the
+// scan, whose per-row counts then place the isolated rows' quads.
 __device__ void plane_count_one(Smem &S, int p) {
 	const int lane = threadIdx.x & 31;
 	const uint32_t lt = (1u << lane) - 1u;
-	uint32_t n_all = 0, n_st[2] = {0, 0};
+	const uint32_t(*m)[4] = S.u.masks[p];
+	const uint32_t rN = m[lane][0], rE = m[lane][1], rD = m[lane][2], rT = m[lane][3];
+	const uint32_t rDup = __shfl_up_sync(0xffffffffu, rD, 1);
+	const bool iso = rD == 0 && (lane == 0 || rDup == 0);
+	const uint32_t icont = rN & (rN << 1) & (rE << 1); // bit v continues the run of v - 1
+	const uint32_t istarts = iso ? (rN & ~icont) : 0u;
+	// per row: quads (low half) and transparent-stream quads (high half), isolated rows only
+	uint32_t itot;
+	const uint32_t iexcl = warp_excl_scan((uint32_t)__popc(istarts) | ((uint32_t)__popc(istarts & rT) << 16), &itot);
+	uint32_t ibase = 0;
+	if (lane == 0 && (itot & 0xffffu))
+		ibase = atomicAdd(&S.misc[4], itot & 0xffffu);
+	ibase = __shfl_sync(0xffffffffu, ibase, 0);
+
+	uint32_t b_all = 0, b_st[2] = {0, 0}; // quads of the scanned rows so far
+	uint32_t mine = 0;                    // lane u: quads of scanned row u (packed like iexcl)
 	const auto reserve = [&](uint32_t starts) {
 		uint32_t b = 0;
 		if (lane == 0)
 			b = atomicAdd(&S.misc[4], (uint32_t)__popc(starts));
 		return b;
 	};
-	warp_merge_plane(S.u.masks[p], reserve, [&](uint32_t b, int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
-		const uint32_t cnt = __popc(starts);
+	warp_merge_plane(m, reserve, [&](uint32_t b, int u, uint32_t starts, uint32_t tmask, bool is_start, int w, int h) {
+		const uint32_t cnt = __popc(starts), c1 = __popc(starts & tmask);
 		const uint32_t base = __shfl_sync(0xffffffffu, b, 0);
+		const uint32_t ex = __shfl_sync(0xffffffffu, iexcl, u); // isolated quads of the rows above u
 		if (is_start) {
 			const int st = (int)((tmask >> lane) & 1u);
 			const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
-			const uint32_t li = n_all + __popc(starts & lt), lk = n_st[st] + __popc(same & lt);
+			const uint32_t ex_all = ex & 0xffffu, ex_t = ex >> 16;
+			const uint32_t li = ex_all + b_all + __popc(starts & lt);
+			const uint32_t lk = (st ? ex_t + b_st[1] : ex_all - ex_t + b_st[0]) + __popc(same & lt);
 			put_record(S, base + __popc(starts & lt), quad_record(p, u, lane, w, h, st, li, lk));
 		}
-		n_all += cnt;
-		n_st[1] += __popc(starts & tmask);
-		n_st[0] += __popc(starts & ~tmask);
-	});
+		if (lane == u)
+			mine = cnt | (c1 << 16);
+		b_all += cnt;
+		b_st[1] += c1;
+		b_st[0] += cnt - c1;
+	}, __ballot_sync(0xffffffffu, !iso));
+
+	// the isolated rows' quads, lane = row
+	uint32_t btot;
+	const uint32_t e = iexcl + warp_excl_scan(mine, &btot);
+	const uint32_t e_all = e & 0xffffu, e_t = e >> 16;
+	uint32_t j = ibase + (iexcl & 0xffffu), k_all = 0, k_t = 0;
+	for (uint32_t rest = istarts; rest; rest &= rest - 1u) {
+		const int v = __ffs(rest) - 1;
+		const uint32_t after = v == 31 ? 0u : (icont >> (v + 1));
+		const int w = __ffs(~after); // cells from v to the end of its run
+		const int st = (int)((rT >> v) & 1u);
+		const uint32_t lk = st ? e_t + k_t : e_all - e_t + (k_all - k_t);
+		put_record(S, j + k_all, quad_record(p, lane, v, w, 1, st, e_all + k_all, lk));
+		++k_all;
+		k_t += (uint32_t)st;
+	}
 	if (lane == 0) {
-		S.seg_cnt[0][1 + p] = n_st[0];
-		S.seg_cnt[1][1 + p] = n_st[1];
+		const uint32_t t1 = (itot >> 16) + b_st[1];
+		S.seg_cnt[0][1 + p] = (itot & 0xffffu) - (itot >> 16) + b_st[0];
+		S.seg_cnt[1][1 + p] = t1;
 	}
 }
 
