@@ -1,5 +1,6 @@
 // Device-side tables, shared-memory layout and small helpers of the GB300 chunk mesher.
 #pragma once
+#include <cstddef>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -156,6 +157,8 @@ struct Smem {
 	uint8_t order[kPlanes];       // the face planes by falling face count: the order they are taken in
 	uint8_t row_of[kWarps][32];   // per warp, key pass: the row whose faces start at each lane of a batch
 };
+
+static_assert(offsetof(Smem, u) % 16 == 0, "plane mask rows are written as 16-byte words");
 
 __device__ __forceinline__ int cls_index(int x, int y, int z) { return ((y + 1) * kCls + (z + 1)) * kCls + (x + 1); }
 __device__ __forceinline__ int lt_index(int x, int y, int z) { return ((y + 1) * kLt + (z + 1)) * kLt + (x + 1); }

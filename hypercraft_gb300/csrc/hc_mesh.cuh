@@ -50,17 +50,22 @@ __device__ int order_planes(Smem &S) {
 			weight[p] = w;
 	}
 	__syncthreads();
-	if (threadIdx.x < kPlanes) {
-		const int p = threadIdx.x;
-		const uint32_t w = weight[p];
+	{ // rank of plane p = planes before it; four neighbouring threads count a quarter each
+		const int p = threadIdx.x >> 2, part = threadIdx.x & 3;
+		const uint32_t w = p < kPlanes ? weight[p] : 0u;
 		int rank = 0;
-		for (int q = 0; q < kPlanes; ++q) {
-			const uint32_t wq = weight[q];
-			rank += (wq > w) || (wq == w && q < p);
+		if (p < kPlanes)
+			for (int q = part; q < kPlanes; q += 4) {
+				const uint32_t wq = weight[q];
+				rank += (wq > w) || (wq == w && q < p);
+			}
+		rank += __shfl_xor_sync(0xffffffffu, rank, 1);
+		rank += __shfl_xor_sync(0xffffffffu, rank, 2);
+		if (p < kPlanes && part == 0) {
+			S.order[rank] = (uint8_t)p;
+			if (w == 0)
+				S.plane_owner[p] = 0;
 		}
-		S.order[rank] = (uint8_t)p;
-		if (w == 0)
-			S.plane_owner[p] = 0;
 	}
 	return __syncthreads_count(threadIdx.x < kPlanes && weight[threadIdx.x] > 0);
 }
@@ -430,6 +435,21 @@ __device__ void custom_emit(Smem &S, const Emit &E, int first, uint32_t ko, uint
 
 __device__ __forceinline__ int plane_id(int axis, int slice, int inv) { return axis * 66 + slice * 2 + inv; }
 
+// 32 x 32 bit transpose across a warp: lane r holds row r (bit c = column c) on entry and column r
+// (bit c = row c) on return. Five butterfly rounds swap ever smaller off-diagonal blocks.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+	const int lane = threadIdx.x & 31;
+	uint32_t m = 0x0000ffffu;
+#pragma unroll
+	for (int j = 16; j != 0; j >>= 1, m ^= m << j) {
+		const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+		const bool upper = (lane & j) != 0;
+		const uint32_t t = (((upper ? y : x) >> j) ^ (upper ? x : y)) & m;
+		x ^= upper ? t : (t << j);
+	}
+	return x;
+}
+
 // Pass 1 (before the relight): visibility of both face planes of every slice from the opaque-cube
 // and blank planes. Between an opaque cube and a blank block only the cube's face shows; two cubes
 // or two blanks show nothing (BlockTexture::Show); any pair involving another block ("complex":
@@ -453,23 +473,25 @@ __device__ void plane_visibility(Smem &S) {
 		mA[0] = va, mA[1] = s != 0 ? cx : 0u, mA[3] = 0;
 		mB[0] = vb, mB[1] = s != 32 ? cx : 0u, mB[3] = 0;
 	}
-	// x slices: per row y, lane = z holds the x-row words; faces of every slice at once, then a
-	// ballot per slice transposes them into plane rows over z
+	// x slices: per row y, lane = z holds the x-row words with the faces of every slice (bit s);
+	// a warp bit transpose turns slices 0-31 into plane rows over z (lane = slice), a ballot slice
+	// 32. Row words are written whole: the equal-below word is cleared again by the key pass.
 	for (int y = warp; y < kChunk; y += kWarps) {
 		const int r = (lane + 1) + kCls * (y + 1);
 		const uint64_t oc = S.aux.pl.oc[r], em = S.aux.pl.em[r];
 		const uint64_t fa = oc & (em >> 1), fb = (oc >> 1) & em; // bit s: face at slice s
 		const uint64_t c = ~(oc | em) & k34, cxp = c | (c >> 1);
-		for (int s = 0; s <= kChunk; ++s) {
-			const uint32_t va = __ballot_sync(0xffffffffu, (fa >> s) & 1u);
-			const uint32_t vb = __ballot_sync(0xffffffffu, (fb >> s) & 1u);
-			const uint32_t cx = __ballot_sync(0xffffffffu, (cxp >> s) & 1u);
-			if (lane == 0) {
-				uint32_t *mA = S.u.masks[plane_id(0, s, 0)][y];
-				uint32_t *mB = S.u.masks[plane_id(0, s, 1)][y];
-				mA[0] = s != 0 ? va : 0u, mA[1] = s != 0 ? cx : 0u, mA[3] = 0;
-				mB[0] = s != 32 ? vb : 0u, mB[1] = s != 32 ? cx : 0u, mB[3] = 0;
-			}
+		const uint32_t va = warp_transpose32((uint32_t)fa), vb = warp_transpose32((uint32_t)fb);
+		const uint32_t cx = warp_transpose32((uint32_t)cxp);
+		const uint32_t va32 = __ballot_sync(0xffffffffu, (fa >> 32) & 1u);
+		const uint32_t cx32 = __ballot_sync(0xffffffffu, (cxp >> 32) & 1u);
+		const int sl = lane; // slices 0-31: face B always, face A from slice 1
+		*reinterpret_cast<uint4 *>(S.u.masks[plane_id(0, sl, 0)][y]) =
+		    sl != 0 ? make_uint4(va, cx, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
+		*reinterpret_cast<uint4 *>(S.u.masks[plane_id(0, sl, 1)][y]) = make_uint4(vb, cx, 0u, 0u);
+		if (lane == 0) { // slice 32: face A only
+			*reinterpret_cast<uint4 *>(S.u.masks[plane_id(0, 32, 0)][y]) = make_uint4(va32, cx32, 0u, 0u);
+			*reinterpret_cast<uint4 *>(S.u.masks[plane_id(0, 32, 1)][y]) = make_uint4(0u, 0u, 0u, 0u);
 		}
 	}
 }
@@ -636,21 +658,6 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live) {
 	}
 }
 
-// 32 x 32 bit transpose across a warp: lane r holds row r (bit c = column c) on entry and column r
-// (bit c = row c) on return. Five butterfly rounds swap ever smaller off-diagonal blocks.
-__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
-	const int lane = threadIdx.x & 31;
-	uint32_t m = 0x0000ffffu;
-#pragma unroll
-	for (int j = 16; j != 0; j >>= 1, m ^= m << j) {
-		const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
-		const bool upper = (lane & j) != 0;
-		const uint32_t t = (((upper ? y : x) >> j) ^ (upper ? x : y)) & m;
-		x ^= upper ? t : (t << j);
-	}
-	return x;
-}
-
 // Exact greedy scan of one plane from its masks (BlockMeshAlgo.hpp:345-477), one warp per plane.
 // For each row u (in order) the quads starting in row u are its runs: maximal stretches of live
 // (visible, not yet covered) cells whose right neighbours are equal (width first); every run then
@@ -669,11 +676,14 @@ template <typename G, typename F>
 __device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], G &&on_starts, F &&on_row,
                                                  uint32_t only = 0xffffffffu) {
 	const int lane = threadIdx.x & 31;
-	const uint32_t rN = m[lane][0], rE = m[lane][1], rT = m[lane][3];
+	const uint32_t rN = m[lane][0];
+	uint32_t rows = __ballot_sync(0xffffffffu, rN != 0) & only;
+	if (!rows)
+		return;
+	const uint32_t rE = m[lane][1], rT = m[lane][3];
 	const uint32_t Dc = warp_transpose32(m[lane][2]); // bit r: cell (r, lane) equals cell (r + 1, lane)
 	const uint32_t upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
 	uint32_t Cc = 0;                                   // bit r: cell (r, lane) is covered
-	uint32_t rows = __ballot_sync(0xffffffffu, rN != 0) & only;
 	while (rows) {
 		const int u = __ffs(rows) - 1;
 		rows &= rows - 1;
@@ -767,6 +777,7 @@ __device__ void plane_count_one(Smem &S, int p) {
 		ibase = atomicAdd(&S.misc[4], itot & 0xffffu);
 	ibase = __shfl_sync(0xffffffffu, ibase, 0);
 
+	const uint32_t scanned = __ballot_sync(0xffffffffu, !iso && rN != 0); // rows for the row scan
 	uint32_t b_all = 0, b_st[2] = {0, 0}; // quads of the scanned rows so far
 	uint32_t mine = 0;                    // lane u: quads of scanned row u (packed like iexcl)
 	const auto reserve = [&](uint32_t starts) {
@@ -792,11 +803,11 @@ __device__ void plane_count_one(Smem &S, int p) {
 		b_all += cnt;
 		b_st[1] += c1;
 		b_st[0] += cnt - c1;
-	}, __ballot_sync(0xffffffffu, !iso));
+	}, scanned);
 
 	// the isolated rows' quads, lane = row
 	uint32_t btot;
-	const uint32_t e = iexcl + warp_excl_scan(mine, &btot);
+	const uint32_t e = iexcl + (scanned ? warp_excl_scan(mine, &btot) : 0u);
 	const uint32_t e_all = e & 0xffffu, e_t = e >> 16;
 	uint32_t j = ibase + (iexcl & 0xffffu), k_all = 0, k_t = 0;
 	for (uint32_t rest = istarts; rest; rest &= rest - 1u) {
