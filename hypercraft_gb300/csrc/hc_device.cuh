@@ -15,6 +15,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 32;
 constexpr int kQuadsPerMesh = 16383;       // 65,532 vertices: the uint16 split point (BlockMeshAlgo.hpp:274)
 constexpr int kMaxMeshesPerStream = 48;    // > 720,896 / 16,383
+constexpr int kMaxSplit = 4;                // face planes keyed in two halves, at most
 constexpr int kPlanes = 198;               // 3 axes x 33 slices x 2 face directions
 constexpr int kSlices = 99;
 constexpr int kSegments = kPlanes + 1;     // segment 0 = custom meshes, then the planes in output order
@@ -156,6 +157,11 @@ struct Smem {
 	uint8_t mine[kPlanes];        // the face planes this CTA took, in the order it took them
 	uint8_t order[kPlanes];       // the face planes by falling face count: the order they are taken in
 	uint8_t row_of[kWarps][32];   // per warp, key pass: the row whose faces start at each lane of a batch
+	// face planes keyed in two halves (the heaviest): the visible and complex words of the row above
+	// the second half, the second half's first row, and how many halves are done
+	uint32_t split_side[kMaxSplit][2];
+	uint32_t split_done[kMaxSplit];
+	uint8_t split_row[kMaxSplit];
 };
 
 static_assert(offsetof(Smem, u) % 16 == 0, "plane mask rows are written as 16-byte words");

@@ -498,15 +498,20 @@ __device__ void plane_visibility(Smem &S) {
 
 // Pass 1b: exact Show for the complex candidates of one plane's rows (texture lookups, dynamic
 // liquid textures), and transparent-pass bits of the faces it shows. Lane = plane row. Run by the
-// warp that takes the plane for its keys.
-__device__ __forceinline__ void plane_complex_one(Smem &S, int p) {
+// warp that takes the plane (or half of it) for its keys: rows [lo, r1) are resolved and returned
+// as visible bits (0 for other rows); rows [r0, r1) are written back. Row lo < r0 is the row above
+// a second half, read from its copy `side` (its words in the masks belong to the other half).
+__device__ __forceinline__ uint32_t plane_complex_one(Smem &S, int p, int lo = 0, int r0 = 0, int r1 = 32,
+                                                      const uint32_t *side = nullptr) {
 	const int lane = threadIdx.x & 31;
 	uint32_t *m = S.u.masks[p][lane];
-	uint32_t cx = m[1];
+	const bool in = lane >= lo && lane < r1, ctx = lane < r0;
+	uint32_t vis = in ? (ctx ? side[0] : m[0]) : 0u;
+	uint32_t cx = in ? (ctx ? side[1] : m[1]) : 0u;
 	if (!__any_sync(0xffffffffu, cx != 0))
-		return;
+		return vis;
 	const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
-	uint32_t vis = m[0], tp = 0;
+	uint32_t tp = 0;
 	while (cx) {
 		const int v = __ffs(cx) - 1;
 		cx &= cx - 1;
@@ -524,9 +529,12 @@ __device__ __forceinline__ void plane_complex_one(Smem &S, int p) {
 			vis &= ~(1u << v);
 		}
 	}
-	m[0] = vis;
-	m[3] = tp;
+	if (in && !ctx) {
+		m[0] = vis;
+		m[3] = tp;
+	}
 	__syncwarp();
+	return vis;
 }
 
 // Position of the n-th (0-based) set bit of mask (n < popc(mask)), by halving the search window.
@@ -575,19 +583,90 @@ __device__ __forceinline__ Key face_key(const Smem &S, int a, int s, int inv, in
 
 __device__ void plane_count_one(Smem &S, int p);
 
+// Warp exclusive prefix sum over lanes of a value packing two 16-bit counts; *total gets the sum.
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t x, uint32_t *total) {
+	const int lane = threadIdx.x & 31;
+	uint32_t incl = x;
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+		if (lane >= d)
+			incl += o;
+	}
+	*total = __shfl_sync(0xffffffffu, incl, 31);
+	return incl - x;
+}
+
+// Heavy face planes (weight >= kSplitMin, the kMaxSplit heaviest) are keyed in two row halves by
+// two warps, so that the heaviest plane does not hold the key phase open; the warp that finishes
+// second merges and counts the plane. The split row balances the weights (visible faces and complex
+// candidates) of the halves. The row above the second half is keyed by both: the second half reads
+// its visible and complex words from a copy taken here, as the first half rewrites them.
+constexpr uint32_t kSplitMin = 128;
+
+// After order_planes (plane weights in seg_base). Returns how many planes are split (every thread).
+__device__ int split_heavy_planes(Smem &S, int live) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t *weight = &S.seg_base[0][0];
+	if (warp < kMaxSplit && warp < live && weight[S.order[warp]] >= kSplitMin) {
+		const int p = S.order[warp];
+		const uint32_t w = __popc(S.u.masks[p][lane][0] | S.u.masks[p][lane][1]);
+		uint32_t tot;
+		const uint32_t ex = warp_excl_scan(w, &tot);
+		const int r = max(__ffs(__ballot_sync(0xffffffffu, 2 * (ex + w) > tot)) - 1, 1);
+		if (lane == 0) {
+			S.split_row[warp] = (uint8_t)r;
+			S.split_side[warp][0] = S.u.masks[p][r - 1][0];
+			S.split_side[warp][1] = S.u.masks[p][r - 1][1];
+			S.split_done[warp] = 0;
+		}
+	}
+	return __syncthreads_count((int)threadIdx.x < kMaxSplit && (int)threadIdx.x < live &&
+	                           weight[S.order[threadIdx.x]] >= kSplitMin);
+}
+
+// Next key-pass item for the calling warp: plane | part << 8 | split index << 10, part 0 = the whole
+// plane, 1 / 2 = the first / second half of split plane k. The halves of the split planes come
+// first, then the other planes heaviest first. A whole plane is recorded as this CTA's when taken,
+// a split one by the warp that merges it.
+__device__ __forceinline__ int claim_item(Smem &S, const Split &sp, int live, int nsplit) {
+	if (sp.c > 1)
+		return claim_plane(S, sp, live);
+	int r = kPlanes;
+	if ((threadIdx.x & 31) == 0) {
+		const int j = (int)atomicAdd(&S.misc[kClaimKeys], 1u);
+		if (j < 2 * nsplit) {
+			r = (int)S.order[j >> 1] | ((1 + (j & 1)) << 8) | ((j >> 1) << 10);
+		} else {
+			const int jj = j - nsplit;
+			r = jj < live ? (int)S.order[jj] : kPlanes;
+			if (r < kPlanes)
+				S.mine[atomicAdd(&S.misc[kMine], 1u)] = (uint8_t)r;
+		}
+	}
+	return __shfl_sync(0xffffffffu, r, 0);
+}
+
+__device__ void plane_count_one(Smem &S, int p);
+
 // Pass 2 (after the relight): equal-to-right and equal-to-below masks of every plane, each plane
 // then merged and counted by the warp that built its masks (no block barrier in between). The visible
 // faces of a plane are taken in batches of whole rows (at most 32 faces), one face per lane, so
 // the light keys are computed by full warps; a face's right neighbour is the next lane and its
-// upper neighbour sits in this batch or in the previous one.
-__device__ void plane_keys(Smem &S, const Split &sp, int live) {
+// upper neighbour sits in this batch or in the previous one. A half plane keys rows [lo, r1) and
+// writes the equal-right bits of rows [r0, r1) and the equal-below bits of rows [lo, r1 - 1).
+__device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int p = claim_plane(S, sp, live); p < kPlanes; p = claim_plane(S, sp, live)) {
-		plane_complex_one(S, p);
+	for (int item = claim_item(S, sp, live, nsplit); (item & 255) < kPlanes; item = claim_item(S, sp, live, nsplit)) {
+		const int p = item & 255, part = (item >> 8) & 3, ks = item >> 10;
+		const int r0 = part == 2 ? (int)S.split_row[ks] : 0, r1 = part == 1 ? (int)S.split_row[ks] : 32;
+		const int lo = r0 > 0 ? r0 - 1 : 0;
+		const uint32_t N = plane_complex_one(S, p, lo, r0, r1, part == 2 ? S.split_side[ks] : nullptr);
 		uint32_t *mrow = S.u.masks[p][lane];
-		const uint32_t N = mrow[0];
-		mrow[1] = 0;
-		mrow[2] = 0;
+		if (lane >= r0 && lane < r1)
+			mrow[1] = 0;
+		if (lane >= lo && (lane < r1 - 1 || (lane == 31 && r1 == 32)))
+			mrow[2] = 0;
 		const uint32_t cnt = __popc(N);
 		uint32_t incl = cnt;
 #pragma unroll
@@ -599,8 +678,6 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live) {
 		const uint32_t start = incl - cnt;
 		const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
 		__syncwarp();
-		if (total == 0)
-			continue;
 		const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
 		Key prev{0, 0, 0};
 		uint32_t prev_b = 0, b = 0;
@@ -634,12 +711,12 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live) {
 			// right neighbour: next lane when (u, v + 1) is visible
 			const Key right = shfl_down_key(key);
 			const bool rv = has && v < 31 && ((Nu >> (v + 1)) & 1u);
-			if (rv && key_eq(key, right))
+			if (rv && u >= r0 && key_eq(key, right))
 				atomicOr(&S.u.masks[p][u][1], 1u << v);
 			// upper neighbour (u - 1, v)
 			const uint32_t Nup = __shfl_sync(0xffffffffu, N, (u + 31) & 31);
 			const uint32_t sup = __shfl_sync(0xffffffffu, start, (u + 31) & 31);
-			const bool uv = has && u > 0 && ((Nup >> v) & 1u);
+			const bool uv = has && u > lo && ((Nup >> v) & 1u);
 			const uint32_t fi = sup + __popc(Nup & ((1u << v) - 1u));
 			const int src_cur = (int)(fi - b) & 31, src_prev = (int)(fi - prev_b) & 31;
 			const Key kc{__shfl_sync(0xffffffffu, key.tex_ao, src_cur), __shfl_sync(0xffffffffu, key.sun, src_cur),
@@ -654,7 +731,22 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live) {
 			ub = ue;
 		}
 		__syncwarp();
-		plane_count_one(S, p);
+		if (part == 0) {
+			if (total != 0)
+				plane_count_one(S, p);
+			continue;
+		}
+		// a half: the warp that finishes second merges the plane (its masks are complete then)
+		__threadfence_block();
+		uint32_t first_done = 0;
+		if (lane == 0)
+			first_done = atomicAdd(&S.split_done[ks], 1u);
+		if (__shfl_sync(0xffffffffu, first_done, 0) == 1u) {
+			__threadfence_block();
+			if (lane == 0)
+				S.mine[atomicAdd(&S.misc[kMine], 1u)] = (uint8_t)p;
+			plane_count_one(S, p);
+		}
 	}
 }
 
@@ -736,20 +828,6 @@ __device__ __forceinline__ void put_record(Smem &S, uint32_t j, uint2 r) {
 }
 __device__ __forceinline__ uint2 get_record(const Smem &S, uint32_t j) {
 	return j < (uint32_t)kQuadBuf ? S.aux.quads[j] : S.spill[j - kQuadBuf];
-}
-
-// Warp exclusive prefix sum over lanes of a value packing two 16-bit counts; *total gets the sum.
-__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t x, uint32_t *total) {
-	const int lane = threadIdx.x & 31;
-	uint32_t incl = x;
-#pragma unroll
-	for (int d = 1; d < 32; d <<= 1) {
-		const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
-		if (lane >= d)
-			incl += o;
-	}
-	*total = __shfl_sync(0xffffffffu, incl, 31);
-	return incl - x;
 }
 
 // Counts the quads of plane p (the calling warp) and keeps their records; misc[4] = records kept.
@@ -1072,9 +1150,10 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		plane_visibility(S);
 		__syncthreads();
 		const int live = order_planes(S);
+		const int nsplit = sp.c > 1 ? 0 : split_heavy_planes(S, live);
 		if (sp.c > 1) // CTA 0's plane counter was reset for this chunk before any CTA takes from it
 			cooperative_groups::this_cluster().sync();
-		plane_keys(S, sp, live); // with each plane's quad count and records
+		plane_keys(S, sp, live, nsplit); // with each plane's quad count and records
 		if (tid == 0) {
 			S.seg_cnt[0][0] = to;
 			S.seg_cnt[1][0] = tt;
