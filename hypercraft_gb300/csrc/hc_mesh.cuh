@@ -1054,39 +1054,38 @@ __device__ void block_scan2(Smem &S, uint32_t a, uint32_t b, uint32_t &ea, uint3
 	__syncthreads();
 }
 
-// Exclusive prefix of the per-segment counts in output order (custom, then planes 0..197).
+// Exclusive prefix of the per-segment counts in output order (custom, then planes 0..197): one
+// thread per segment, a warp scan each, then the warp totals. Called by every thread; the caller
+// syncs before reading the result.
 __device__ void segment_scan(Smem &S) {
-	if (threadIdx.x >= 32)
-		return;
-	const int lane = threadIdx.x;
-	constexpr int kPer = (kSegments + 31) / 32;
-	uint32_t so = 0, stt = 0;
-	for (int i = 0; i < kPer; ++i) {
-		const int sidx = lane * kPer + i;
-		if (sidx < kSegments)
-			so += S.seg_cnt[0][sidx], stt += S.seg_cnt[1][sidx];
-	}
+	constexpr int kScanWarps = (kSegments + 31) / 32;
+	static_assert(kScanWarps <= kWarps, "one thread per segment");
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const bool in = tid < kSegments;
+	const uint32_t so = in ? S.seg_cnt[0][tid] : 0u, stt = in ? S.seg_cnt[1][tid] : 0u;
 	uint32_t io = so, it = stt;
+	if (warp < kScanWarps) {
 #pragma unroll
-	for (int d = 1; d < 32; d <<= 1) {
-		const uint32_t xo = __shfl_up_sync(0xffffffffu, io, d), xt = __shfl_up_sync(0xffffffffu, it, d);
-		if (lane >= d)
-			io += xo, it += xt;
-	}
-	uint32_t bo = io - so, bt = it - stt;
-	for (int i = 0; i < kPer; ++i) {
-		const int sidx = lane * kPer + i;
-		if (sidx < kSegments) {
-			S.seg_base[0][sidx] = bo;
-			S.seg_base[1][sidx] = bt;
-			S.seg_base[2][sidx] = bo + bt;
-			bo += S.seg_cnt[0][sidx];
-			bt += S.seg_cnt[1][sidx];
+		for (int d = 1; d < 32; d <<= 1) {
+			const uint32_t xo = __shfl_up_sync(0xffffffffu, io, d), xt = __shfl_up_sync(0xffffffffu, it, d);
+			if (lane >= d)
+				io += xo, it += xt;
 		}
+		if (lane == 31)
+			S.warp_sum[0][warp] = io, S.warp_sum[1][warp] = it;
 	}
-	if (lane == 31) {
-		S.misc[0] = io; // opaque quads
-		S.misc[1] = it; // transparent quads
+	__syncthreads();
+	if (in) {
+		uint32_t bo = io - so, bt = it - stt;
+		for (int w = 0; w < warp; ++w)
+			bo += S.warp_sum[0][w], bt += S.warp_sum[1][w];
+		S.seg_base[0][tid] = bo;
+		S.seg_base[1][tid] = bt;
+		S.seg_base[2][tid] = bo + bt;
+		if (tid == kSegments - 1) {
+			S.misc[0] = bo + so; // opaque quads
+			S.misc[1] = bt + stt; // transparent quads
+		}
 	}
 }
 
