@@ -211,6 +211,13 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 		asm volatile("cp.async.commit_group;" ::: "memory");
 		for (int i = threadIdx.x; i < 256; i += kThreads)
 			S.classes[i] = T.classes[i];
+		// With the batch light pass's level planes the light bytes are decoded now, their loads
+		// overlapping the copies; the class ids then go into the high bytes of the cells alone.
+		// Otherwise the whole cell is written (light 0 for the relight to raise).
+		const bool lit = S.lvl[26] != nullptr;
+		uint8_t *const hi = reinterpret_cast<uint8_t *>(S.cell) + 1;
+		if (lit)
+			light_from_levels(S);
 		// Meanwhile, one thread per row of [-1, 32]^2: the opaque-cube and blank bits of the row from
 		// its chunk's planes with the x = -1 and x = 32 bits from the x neighbours' (bit x + 1), and
 		// the class ids of the row's two edge cells.
@@ -223,8 +230,13 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 			const uint8_t e0 = class_byte(S, -1, y, z), e1 = class_byte(S, kChunk, y, z);
 			S.aux.pl.oc[row] = (uint64_t)(ocm >> 31) | ((uint64_t)oc << 1) | ((uint64_t)(ocp & 1u) << 33);
 			S.aux.pl.em[row] = (uint64_t)(emm >> 31) | ((uint64_t)em << 1) | ((uint64_t)(emp & 1u) << 33);
-			S.cell[row * kCls] = (uint16_t)(e0 << 8);
-			S.cell[row * kCls + kCls - 1] = (uint16_t)(e1 << 8);
+			if (lit) {
+				hi[2 * (row * kCls)] = e0;
+				hi[2 * (row * kCls + kCls - 1)] = e1;
+			} else {
+				S.cell[row * kCls] = (uint16_t)(e0 << 8);
+				S.cell[row * kCls + kCls - 1] = (uint16_t)(e1 << 8);
+			}
 		}
 		asm volatile("cp.async.wait_group 0;" ::: "memory");
 		__syncthreads();
@@ -243,7 +255,10 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 			for (int j = 0; j < kBatch; ++j) {
 				if (row0 + j >= kRows) // the same for the whole warp
 					break;
-				S.cell[(row0 + j) * kCls + lane + 1] = (uint16_t)(c[j] << 8);
+				if (lit)
+					hi[2 * ((row0 + j) * kCls + lane + 1)] = c[j];
+				else
+					S.cell[(row0 + j) * kCls + lane + 1] = (uint16_t)(c[j] << 8);
 			}
 		}
 		__syncthreads();
@@ -1141,10 +1156,10 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		if (lead && has_custom) // no inner block with a custom mesh: nothing to count
 			custom_count(S, tid * kBlocksPerThread, co, ct);
 		block_scan2(S, co, ct, eo, et, to, tt);
-		if (S.lvl[26])
-			light_from_levels(S);
-		else
+		if (!S.lvl[26])
 			relight_window(S, T, sp); // the relight scratch shares memory with the plane masks
+		else if (!S.pln[26])
+			light_from_levels(S); // with chunk planes the staging decoded the light
 		__syncthreads();
 		plane_visibility(S);
 		__syncthreads();
