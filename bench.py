@@ -78,7 +78,7 @@ def workload_name(args):
 
 # DRAM bytes (read + write) of one k_mesh_batch launch on the default scale workload, from one
 # ncu capture (profiles/k_mesh_batch_scale32x8x32_dram.md gives the command); other workloads: null
-MESH_TRAFFIC_BYTES = {"scale:32x8x32": 1.534e9}
+MESH_TRAFFIC_BYTES = {"scale:32x8x32": 1.496e9}
 
 
 def mesh_traffic(args):
