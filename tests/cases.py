@@ -128,6 +128,43 @@ def vines_and_plants():
     return b, h
 
 
+def _slab(centre_top):
+    """27 chunks of flat ground: the centre layer of chunks is stone below y = 10 with `centre_top`
+    (a function of the cell arrays giving the raw block at y = 10) on top, sunlit above; the layer
+    above is air, the one below stone."""
+    b, h = [], []
+    for i in range(27):
+        cy = (i // 3) % 3  # 0: the layer above, 1: below, 2: the centre's
+        if cy == 0:
+            b.append(np.zeros(N, np.uint16)), h.append(np.zeros(1024, np.int8))
+        elif cy == 1:
+            b.append(np.ones(N, np.uint16)), h.append(np.full(1024, 32, np.int8))
+        else:
+            b.append(np.where(Y < 10, 1, np.where(Y == 10, 4, 0)).astype(np.uint16))
+            h.append(np.full(1024, 11, np.int8))
+    b[26] = np.where(Y < 10, 1, np.where(Y == 10, centre_top(X, Z), 0)).astype(np.uint16)
+    return b, h
+
+
+def flat_ground(leaves: bool):
+    """A flat grass top: its face plane holds 1,024 faces (keyed in two halves) that merge into one
+    quad across the split row; with leaves on the rows around the split (z = 14..16), the row above
+    the second half holds complex faces."""
+    b, h = _slab(lambda x, z: np.full(x.shape, 4))
+    if leaves:
+        for x, z in [(3, 15), (4, 15), (9, 15), (20, 15), (31, 15), (0, 16), (12, 16), (7, 14), (25, 14)]:
+            b[26][x + (11 * 32 + z) * 32] = 16
+    return b, h
+
+
+def stripes():
+    """Grass and dirt tops in z rows: pairs of equal rows (rows linked by equal-below cells) for
+    z < 16, single rows alternating for z >= 16 (isolated rows), and a glass strip."""
+    b, h = _slab(lambda x, z: np.where(z < 16, np.where((z // 2) % 2 == 0, 4, 3), np.where(z % 2 == 0, 4, 3)))
+    b[26][np.flatnonzero((Y == 11) & (X == 5))] = 9
+    return b, h
+
+
 def terrain_sample(kind: str, k: int):
     """Chunk k of a small seeded scale (caves + glowstone) or mixture world."""
     from hypercraft_gb300 import worldgen

@@ -52,6 +52,16 @@ def test_mesh_chunk_matches_oracle_random(ctx, oracle, seed):
             assert a == c
 
 
+@pytest.mark.parametrize("make", [lambda: cases.flat_ground(False), lambda: cases.flat_ground(True), cases.stripes],
+                         ids=["flat_ground", "flat_ground_leaves", "stripes"])
+def test_split_planes_and_isolated_rows_match_oracle(ctx, oracle, make):
+    """A 1,024-face plane keyed in two halves (one quad across the split row; complex faces on the
+    row above the second half) and planes mixing isolated rows with rows linked by equal-below cells."""
+    b, h = make()
+    mg, mo = ctx.mesh_chunk(b, h), oracle.mesh_chunk(b, h)
+    assert len(mg) == len(mo) and all(a == c for a, c in zip(mg, mo))
+
+
 def test_most_quads_match_oracle(ctx, oracle):
     """196,608 quads: past the shared and global record buffers, so the emission merges planes again
     in windows; the result still equals the oracle's."""
