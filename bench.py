@@ -86,6 +86,13 @@ def mesh_traffic(args):
     return MESH_TRAFFIC_BYTES.get(f"{args.workload}:{nx}x{ny}x{nz}")
 
 
+# What bounds k_mesh_batch instead of DRAM: its instruction issue and ALU pipe utilisation from one
+# ncu --set full capture of the same scale terrain at 16x8x16 (profiles/k_mesh_batch_scale16x8x16.md
+# gives the command); the integer merge and light-key work keeps the SMs busy while DRAM idles.
+MESH_ISSUE = {"issue_active_frac": 0.559, "alu_pipe_frac": 0.486, "dram_throughput_frac": 0.074,
+              "warps_active_frac": 0.500, "source": "ncu --set full, k_mesh_batch, scale 16x8x16"}
+
+
 def hbm_peak():
     try:
         with open(PEAKS_FILE) as f:
@@ -451,7 +458,8 @@ def ours(args):
                          "kernel_ms": mesh_ms,
                          "stage_ms": {"planes": float(stages[0]), "light_pass": float(stages[1]),
                                       "mesh": float(stages[2])},
-                         "algorithmic_bytes_per_launch": algo_bytes},
+                         "algorithmic_bytes_per_launch": algo_bytes,
+                         "issue": MESH_ISSUE if args.workload == "scale" and variant == 0 else None},
             "serving": serving,
             # per step the plan's graph runs the plane refresh, the blank test (one-CTA variants), 15 light
             # levels (light-pass variant only) and the mesher
