@@ -395,7 +395,7 @@ __device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hg
 constexpr int kLevels = 15;
 constexpr size_t kLevelSlotWords = (size_t)2 * kLevels * kPlaneWords; // per chunk: 2 channels x 15 levels
 constexpr size_t kEdgeSlotWords = (size_t)2 * kLevels * 2 * 32;       // per chunk: x = 0 and x = 31 bits
-constexpr int kLightThreads = 256;                                     // one block per chunk
+constexpr int kLightThreads = 128;                                     // one block per chunk
 constexpr int kLightRows = kPlaneWords / kLightThreads;                // rows per thread
 
 struct LightPass {
@@ -449,7 +449,7 @@ __device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
 // read at the next level, and the plane's uniform bits (LightPass::flags). A channel whose level
 // follows from level t + 1 without computing (see kFlag*) is skipped: a chunk of sunlit air far
 // from any emitter costs one flag word per level.
-__global__ void __launch_bounds__(kLightThreads, 8) k_light_level(LightPass L, DevTables T, int t) {
+__global__ void __launch_bounds__(kLightThreads, 16) k_light_level(LightPass L, DevTables T, int t) {
 	__shared__ __align__(16) uint32_t prev[2][kPlaneWords];
 	__shared__ uint32_t side[2][6][32]; // per channel: -x hi edge, +x lo edge, -y rows, +y rows, -z rows, +z rows
 	__shared__ int s_nb[6];
