@@ -121,6 +121,28 @@ class Arena:
                                  bool(d["transparent"])))
         return out
 
+    def sample_meshes(self, positions) -> dict:
+        """{batch position: its meshes} for the given positions, reading back only their descriptor
+        and vertex/index ranges (a full-size arena holds gigabytes)."""
+        n = self.n
+        res = self.results[:5 * n].cpu().numpy().view(np.uint32).reshape(-1, 5)
+        out = {}
+        for i in positions:
+            r = res[int(i)]
+            if r[4] != RESULT_OK:
+                raise HcError(int(r[4]), f"chunk {int(i)} status {int(r[4])}")
+            d0, dn = int(r[2]), int(r[3])
+            descs = self.meshes[12 * d0:12 * (d0 + dn)].cpu().numpy().view(MESH_DESC_DTYPE)
+            meshes = []
+            for d in descs:
+                vo, vc, io, ic = (int(d[k]) for k in ("vertex_offset", "vertex_count", "index_offset", "index_count"))
+                v = self.vertices[2 * vo:2 * (vo + vc)].cpu().numpy().view(np.uint32).reshape(-1, 2)
+                ix = self.indices[io:io + ic].cpu().numpy().view(np.uint16)
+                meshes.append(BlockMesh(v, ix, tuple(int(x) for x in d["aabb_min"]) + tuple(int(x) for x in d["aabb_max"]),
+                                        bool(d["transparent"])))
+            out[int(i)] = meshes
+        return out
+
     def results_host(self, n: int) -> np.ndarray:
         """The first n chunks' result words, (n, 5) uint32."""
         return self.results[:5 * n].cpu().numpy().view(np.uint32).reshape(-1, 5)

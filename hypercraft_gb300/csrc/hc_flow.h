@@ -1,6 +1,6 @@
 // Flowing-liquid dynamic mesh, shared by the host registry and the device mesher.
 //
-// Restates block/block/public/Liquid.hpp:266-397 (flow_mesh_gen<WaterTrait, Variant>) for water
+// Restates block/block/public/Liquid.hpp:151-282 (get_flow_height, flow_mesh_gen<WaterTrait, Variant>) for water
 // (Water.hpp:5-14): neighbour heights from the eight horizontal neighbours in fetch order
 // (-1,-1) (0,-1) (1,-1) (-1,0) (1,0) (-1,1) (0,1) (1,1) as (dx, dz), corner heights, the sloped top
 // face, up to four side faces, and the six textures that replace the block's own face textures.

@@ -4,7 +4,6 @@
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
-#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -417,64 +416,75 @@ hc_status fail(hc_ctx *ctx, hc_status s, const std::string &msg) {
 			            std::string(#call) + ": " + cudaGetErrorString(e_));                                               \
 	} while (0)
 
-// Derives the block classes from the registry: each distinct device row gets one id.
+// The device row of one raw block value: face textures, light-pass and shape flags, tag, light level
+// and custom-mesh fields.
+DevClass class_row(const hc_block_props &p) {
+	DevClass d;
+	std::memset(&d, 0, sizeof(d));
+	bool all_empty = true, all_opaque = true;
+	for (int f = 0; f < 6; ++f) {
+		d.tex[f] = p.tex[f];
+		const bool empty = (p.tex[f] & 0x1fffu) == 0;
+		all_empty &= empty;
+		all_opaque &= !empty && !hc_tex_is_transparent(p.tex[f]);
+	}
+	const bool vertical = p.transparency == HC_TRANSPARENT;
+	uint8_t flags = 0;
+	if (p.transparency != HC_OPAQUE)
+		flags |= kFIndirect;
+	if (vertical || p.collision != HC_COLLISION_SOLID)
+		flags |= kFDirect;
+	if (vertical)
+		flags |= kFVertical;
+	if (p.mesh_kind == HC_MESH_NONE && all_opaque)
+		flags |= kFOpaqueCube;
+	if (p.mesh_kind == HC_MESH_NONE && all_empty)
+		flags |= kFEmpty;
+	const uint8_t tag = p.id == HC_BLK_AIR             ? kTagAir
+	                    : p.id == HC_BLK_WATER         ? kTagSource
+	                    : p.id == HC_BLK_FLOWING_WATER ? kTagFlow
+	                                                   : kTagOther;
+	d.flags = (uint8_t)(flags | (tag << kFTagShift));
+	d.light = p.light_level;
+	d.mesh_first = p.mesh_kind == HC_MESH_STATIC ? p.mesh_first : 0;
+	const uint8_t param = p.mesh_kind == HC_MESH_STATIC ? p.mesh_count : (p.mesh_kind == HC_MESH_FLOW ? p.flow_variant : 0);
+	d.mesh_meta = (uint8_t)(p.mesh_kind | (param << 2));
+	return d;
+}
+
+// Derives the block classes from the registry: each distinct device row gets one id, in order of
+// first appearance within its light-pass group (bit 7 indirect pass, bit 6 direct pass, 64 ids per
+// group). Unused ids repeat the row of raw value 0. Uses no heap, so the context tables and the
+// no-alloc entry point's static tables come from this one routine. False: more than 64 distinct
+// rows in a group.
+bool assign_classes(const hc_registry &reg, uint8_t *class_of, DevClass *classes) {
+	uint32_t count[4] = {0, 0, 0, 0};
+	bool used[256] = {false};
+	for (uint32_t raw = 0; raw < 65536u; ++raw) {
+		const DevClass d = class_row(reg.props[raw]);
+		const uint32_t group = ((d.flags & kFIndirect) ? 2u : 0u) | ((d.flags & kFDirect) ? 1u : 0u);
+		uint32_t c = 0;
+		while (c < count[group] && std::memcmp(&classes[(group << 6) | c], &d, sizeof(d)) != 0)
+			++c;
+		if (c == count[group]) {
+			if (c == 64)
+				return false;
+			classes[(group << 6) | c] = d;
+			used[(group << 6) | c] = true;
+			++count[group];
+		}
+		class_of[raw] = (uint8_t)((group << 6) | c);
+	}
+	for (uint32_t c = 0; c < 256; ++c)
+		if (!used[c])
+			classes[c] = classes[class_of[0]];
+	return true;
+}
+
 bool build_classes(const hc_registry &reg, std::vector<uint8_t> &class_of, std::vector<DevClass> &classes) {
 	class_of.assign(65536, 0);
 	classes.assign(256, DevClass{});
-	std::vector<bool> used(256, false);
-	uint32_t group_count[4] = {0, 0, 0, 0};
-	std::map<std::string, uint8_t> seen;
-	for (uint32_t raw = 0; raw < 65536u; ++raw) {
-		const hc_block_props &p = reg.props[raw];
-		DevClass d;
-		std::memset(&d, 0, sizeof(d));
-		bool all_empty = true, all_opaque = true;
-		for (int f = 0; f < 6; ++f) {
-			d.tex[f] = p.tex[f];
-			const bool empty = (p.tex[f] & 0x1fffu) == 0;
-			all_empty &= empty;
-			all_opaque &= !empty && !hc_tex_is_transparent(p.tex[f]);
-		}
-		const bool vertical = p.transparency == HC_TRANSPARENT;
-		uint8_t flags = 0;
-		if (p.transparency != HC_OPAQUE)
-			flags |= kFIndirect;
-		if (vertical || p.collision != HC_COLLISION_SOLID)
-			flags |= kFDirect;
-		if (vertical)
-			flags |= kFVertical;
-		if (p.mesh_kind == HC_MESH_NONE && all_opaque)
-			flags |= kFOpaqueCube;
-		if (p.mesh_kind == HC_MESH_NONE && all_empty)
-			flags |= kFEmpty;
-		const uint8_t tag = p.id == HC_BLK_AIR ? kTagAir
-		                    : p.id == HC_BLK_WATER ? kTagSource
-		                    : p.id == HC_BLK_FLOWING_WATER ? kTagFlow
-		                                                   : kTagOther;
-		flags |= (uint8_t)(tag << kFTagShift);
-		d.flags = flags;
-		d.light = p.light_level;
-		d.mesh_first = p.mesh_kind == HC_MESH_STATIC ? p.mesh_first : 0;
-		const uint8_t param = p.mesh_kind == HC_MESH_STATIC ? p.mesh_count : (p.mesh_kind == HC_MESH_FLOW ? p.flow_variant : 0);
-		d.mesh_meta = (uint8_t)(p.mesh_kind | (param << 2));
-		std::string key(reinterpret_cast<const char *>(&d), sizeof(d));
-		auto it = seen.find(key);
-		if (it == seen.end()) {
-			// the id carries the light-pass flags: bit 7 indirect, bit 6 direct, 64 ids per pair
-			const uint32_t group = ((flags & kFIndirect) ? 2u : 0u) | ((flags & kFDirect) ? 1u : 0u);
-			if (group_count[group] >= 64)
-				return false;
-			const uint8_t id = (uint8_t)((group << 6) | group_count[group]++);
-			it = seen.emplace(key, id).first;
-			classes[id] = d;
-			used[id] = true;
-		}
-		class_of[raw] = it->second;
-	}
-	for (int i = 0; i < 256; ++i)
-		if (!used[i])
-			classes[i] = classes[class_of[0]];
-	return true;
+	return assign_classes(reg, class_of.data(), classes.data());
 }
 
 hc_status upload_tables(hc_ctx *ctx) {
@@ -1761,65 +1771,12 @@ uint8_t g_noalloc_class_of_host[65536];
 DevClass g_noalloc_classes_host[256];
 bool g_noalloc_tables_built = false;
 
-DevClass noalloc_class_row(const hc_block_props &p) {
-	DevClass d;
-	std::memset(&d, 0, sizeof(d));
-	bool all_empty = true, all_opaque = true;
-	for (int f = 0; f < 6; ++f) {
-		d.tex[f] = p.tex[f];
-		const bool empty = (p.tex[f] & 0x1fffu) == 0;
-		all_empty &= empty;
-		all_opaque &= !empty && !hc_tex_is_transparent(p.tex[f]);
-	}
-	const bool vertical = p.transparency == HC_TRANSPARENT;
-	uint8_t flags = 0;
-	if (p.transparency != HC_OPAQUE)
-		flags |= kFIndirect;
-	if (vertical || p.collision != HC_COLLISION_SOLID)
-		flags |= kFDirect;
-	if (vertical)
-		flags |= kFVertical;
-	if (p.mesh_kind == HC_MESH_NONE && all_opaque)
-		flags |= kFOpaqueCube;
-	if (p.mesh_kind == HC_MESH_NONE && all_empty)
-		flags |= kFEmpty;
-	const uint8_t tag = p.id == HC_BLK_AIR             ? kTagAir
-	                    : p.id == HC_BLK_WATER         ? kTagSource
-	                    : p.id == HC_BLK_FLOWING_WATER ? kTagFlow
-	                                                   : kTagOther;
-	d.flags = (uint8_t)(flags | (tag << kFTagShift));
-	d.light = p.light_level;
-	d.mesh_first = p.mesh_kind == HC_MESH_STATIC ? p.mesh_first : 0;
-	const uint8_t param = p.mesh_kind == HC_MESH_STATIC ? p.mesh_count : (p.mesh_kind == HC_MESH_FLOW ? p.flow_variant : 0);
-	d.mesh_meta = (uint8_t)(p.mesh_kind | (param << 2));
-	return d;
-}
-
 bool noalloc_build_tables() {
 	if (g_noalloc_tables_built)
 		return true;
 	hc_registry_build(&g_noalloc_registry);
-	// same id scheme as the context tables: bit 7 indirect pass, bit 6 direct pass, 64 ids per pair
-	uint32_t count[4] = {0, 0, 0, 0};
-	bool used[256] = {false};
-	for (uint32_t raw = 0; raw < 65536u; ++raw) {
-		const DevClass d = noalloc_class_row(g_noalloc_registry.props[raw]);
-		const uint32_t group = ((d.flags & kFIndirect) ? 2u : 0u) | ((d.flags & kFDirect) ? 1u : 0u);
-		uint32_t c = 0;
-		while (c < count[group] && std::memcmp(&g_noalloc_classes_host[(group << 6) | c], &d, sizeof(d)) != 0)
-			++c;
-		if (c == count[group]) {
-			if (c == 64)
-				return false;
-			g_noalloc_classes_host[(group << 6) | c] = d;
-			used[(group << 6) | c] = true;
-			++count[group];
-		}
-		g_noalloc_class_of_host[raw] = (uint8_t)((group << 6) | c);
-	}
-	for (uint32_t c = 0; c < 256; ++c)
-		if (!used[c])
-			g_noalloc_classes_host[c] = g_noalloc_classes_host[g_noalloc_class_of_host[0]];
+	if (!assign_classes(g_noalloc_registry, g_noalloc_class_of_host, g_noalloc_classes_host))
+		return false;
 	g_noalloc_tables_built = true;
 	return true;
 }
@@ -1839,6 +1796,12 @@ hc_status noalloc_setup(int dev, char *err, size_t err_size) {
 		return HC_OK;
 	if (!noalloc_build_tables()) {
 		noalloc_error(err, err_size, "%smore than 256 distinct block classes");
+		return HC_ERR_INVALID_ARG;
+	}
+	if (g_noalloc_registry.static_face_count > HC_MAX_STATIC_FACES / 4) {
+		noalloc_error(err, err_size, "%stoo many static custom-mesh faces (%llu, at most %llu)", "",
+		              (unsigned long long)g_noalloc_registry.static_face_count,
+		              (unsigned long long)(HC_MAX_STATIC_FACES / 4));
 		return HC_ERR_INVALID_ARG;
 	}
 	uint64_t tt = 0, tl = 0, tp = 0;

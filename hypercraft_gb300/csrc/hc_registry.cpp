@@ -2,13 +2,13 @@
 //
 // Sources restated here (all paths inside the reference project):
 //   texture flags ........ texture/internal/generated/block_texture_transparency.inl:1-3
-//   variant/transform .... block/generator/Block.cpp.in:51-60, block/block/public/Trait.hpp:101-141
+//   variant/transform .... block/generator/Block.cpp.in:9-15, block/block/public/Trait.hpp:24-64
 //   per-id properties .... block/block/*.hpp (air.hpp ... glowstone.hpp)
 //   rotation of logs ..... block/include/block/BlockProperty.hpp:30-75, block/block/log.hpp:26-35
 //   cross meshes ......... block/block/public/CrossMesh.hpp:7-52
 //   inner-surface meshes . block/block/public/InnerSurfaceMesh.hpp:7-43
 //   cactus ............... block/block/cactus.hpp:4-48
-//   liquid flow mesh ..... block/block/public/Liquid.hpp:266-417, Water.hpp:5-14
+//   liquid flow mesh ..... block/block/public/Liquid.hpp:151-155 (heights), 156-282 (faces), 284-302 (kLiquidFlowMesh), Water.hpp:5-14
 #include "hc_registry.h"
 #include "hc_flow.h"
 

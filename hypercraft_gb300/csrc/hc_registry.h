@@ -3,7 +3,7 @@
 // A block is a uint16 `raw = id | meta << 8` (block/include/block/Block.hpp:22-33; the
 // little-endian {m_id, m_meta} layout applies because common/Endian.hpp is never included).
 // Its property row is what the reference's generated 65,536-entry table holds
-// (block/generator/Block.cpp.in:51-76, driven by the per-id traits in block/block/*.hpp):
+// (block/generator/Block.cpp.in:9-27, driven by the per-id traits in block/block/*.hpp):
 // six face textures, transparency, light level, collision and an optional custom mesh.
 //
 // This header restates that table from the trait definitions; the row for every raw value is
@@ -111,7 +111,7 @@ enum { HC_OPAQUE = 0, HC_SEMI_TRANSPARENT = 1, HC_TRANSPARENT = 2 };
 enum { HC_COLLISION_NONE = 0, HC_COLLISION_SOLID = 1, HC_COLLISION_WATER = 2 };
 
 // Custom-mesh kinds. A static mesh is a fixed face list; a flow mesh is computed from the
-// eight horizontal neighbours (block/block/public/Liquid.hpp:271-417).
+// eight horizontal neighbours (block/block/public/Liquid.hpp:156-302).
 enum { HC_MESH_NONE = 0, HC_MESH_STATIC = 1, HC_MESH_FLOW = 2 };
 
 // Block faces (block/include/block/BlockFace.hpp:9-11): +x, -x, +y, -y, +z, -z.
@@ -156,7 +156,7 @@ int hc_tex_is_transparent(uint16_t tex);
 int hc_tex_is_liquid(uint16_t tex);
 int hc_tex_use_transparent_pass(uint16_t tex);
 
-// Flowing-liquid dynamic mesh (block/block/public/Liquid.hpp:271-397): given the raw values of
+// Flowing-liquid dynamic mesh (block/block/public/Liquid.hpp:156-282): given the raw values of
 // the eight horizontal neighbours in fetch order and the clamped variant, writes the faces and
 // the six per-face textures that replace the block's own.
 void hc_flow_mesh(const uint16_t nei[8], uint8_t variant, hc_mesh_face *faces, uint32_t *face_count,

@@ -7,7 +7,7 @@
 // (client/src/ChunkFloodSunlightTask.cpp:33-66) recomputes their heights from the chunk above;
 // kSetSunlight (client/src/ChunkSetSunlightTask.cpp:28-90) stores changed heights, marks the 27
 // chunks around for remeshing and floods the same columns of the chunk below; kGenerate
-// (client/src/ChunkGenerateTask.cpp:22-42) queues kMesh for the chunk it loaded, and kMesh waits
+// (client/src/ChunkGenerateTask.cpp:21-40) queues kMesh for the chunk it loaded, and kMesh waits
 // until all 26 neighbours are loaded (client/src/ChunkMeshTask.cpp:14-39).
 //
 // Here each stage is a kernel over a device list that the stage before it appended to, with the

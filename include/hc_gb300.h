@@ -245,7 +245,7 @@ void hc_world_destroy(hc_world *world);
 hc_status hc_world_apply_edits(hc_world *world, const hc_edit *edits, uint32_t n, int src_on_device, void *stream);
 
 /* A chunk entering the world (replaces ChunkTaskRunner<kGenerate>::Run,
- * client/src/ChunkGenerateTask.cpp:22-42): its generated blocks (32768 uint16) and sunlight
+ * client/src/ChunkGenerateTask.cpp:21-40): its generated blocks (32768 uint16) and sunlight
  * heights (1024 int8), host memory, are copied into pool slot `slot`; then its stored edits are
  * applied in order, as the reference applies a ChunkEntry from its database: block entries in the
  * PackedChunkBlockEntry layout (uint32: cell index << 16 | raw block) and sunlight entries in the
@@ -390,9 +390,13 @@ hc_status hc_server_replay(hc_server *server, const hc_request *requests, const 
  * held until exit). It calls no cudaMalloc, cudaFree or other allocating routine.
  *
  * Limit: 1..HC_NOALLOC_MAX_CHUNKS chunks per call; larger batches return HC_ERR_CAPACITY.
- * The first call on a device (the current one) sets the tables up with synchronous copies. All
- * calls on a device share the scratch, so calls that overlap on the GPU race; run them in one
- * stream or one at a time. Synchronous: it waits for its stream.
+ * Output buffers too small for the batch: HC_ERR_CAPACITY, with the required quad and mesh counts
+ * written to *quads and *mesh_count (the chunks that did not fit have status 1 and no output).
+ * The first call on a device (the current one) sets the tables up with synchronous copies; make
+ * it before any stream capture. The set-up is kept for the life of the process: a device reset
+ * (cudaDeviceReset) discards the tables, so do not call this entry point on a device again after
+ * resetting it. All calls on a device share the scratch, so calls that overlap on the GPU race; run
+ * them in one stream or one at a time. Synchronous: it waits for its stream.
  * results_host (n x 5 words, may be NULL) receives {opaque quads, transparent quads, first mesh,
  * mesh count, status} per chunk; error_text (may be NULL) receives a message.
  * ---------------------------------------------------------------------------------------------- */

@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import shutil
 import subprocess
 from dataclasses import dataclass
 
@@ -18,7 +19,8 @@ BUILD_DIR = os.path.join(ORACLE_DIR, "_build")
 REF_DIR = os.path.join(ORACLE_DIR, "_ref")
 ORACLE_LIB = os.path.join(BUILD_DIR, "libhc_oracle.so")
 REF_LIB = os.path.join(REF_DIR, "libhcref.so")
-REFERENCE_SRC = "/root/reference"
+# the reference headers and generated block table, copied out of a checkout for hosts without one
+BUNDLE_DIR = os.path.join(REF_DIR, "src")
 
 FLAT_WORDS = 9
 
@@ -33,12 +35,58 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_LIB
 
 
+def reference_source() -> str | None:
+    """The reference checkout: $HC_REFERENCE_SRC, else a checkout named ``reference`` beside the
+    repository; None where neither holds the reference's mesher header."""
+    for p in (os.environ.get("HC_REFERENCE_SRC"), os.path.join(os.path.dirname(REPO_DIR), "reference")):
+        if p and os.path.isfile(os.path.join(p, "client", "include", "client", "BlockMeshAlgo.hpp")):
+            return p
+    return None
+
+
+def _make(*args: str) -> None:
+    jobs = str(min(8, os.cpu_count() or 1))
+    subprocess.run(["make", "-s", "-f", "Makefile.ref", f"-j{jobs}", *args], cwd=ORACLE_DIR, check=True)
+
+
+def _bundle(src: str) -> None:
+    """Copies what the harness build reads from the checkout into ``_ref/src``, unmodified and at the
+    same relative paths: the headers the two translation units include (``make deps``), the whole glm
+    tree (it includes other headers on aarch64 than on x86) and the generated Block.cpp. The bundle
+    is git-ignored; it lets a host without the checkout build the same library."""
+    stamp = os.path.join(BUNDLE_DIR, ".complete")
+    if os.path.exists(stamp):
+        return
+    out = subprocess.run(["make", "-s", "-f", "Makefile.ref", f"REF={src}", "deps"], cwd=ORACLE_DIR, check=True,
+                         capture_output=True, text=True).stdout
+    root = os.path.realpath(src)
+    for line in out.split():
+        f = os.path.realpath(os.path.join(ORACLE_DIR, line))
+        if not f.startswith(root + os.sep):
+            continue  # the harness's own files and system headers
+        dst = os.path.join(BUNDLE_DIR, os.path.relpath(f, root))
+        os.makedirs(os.path.dirname(dst), exist_ok=True)
+        shutil.copyfile(f, dst)
+    shutil.copytree(os.path.join(root, "dep", "glm"), os.path.join(BUNDLE_DIR, "dep", "glm"), dirs_exist_ok=True)
+    shutil.copyfile(os.path.join(REF_DIR, "Block.cpp"), os.path.join(BUNDLE_DIR, "Block.cpp"))
+    open(stamp, "w").close()
+
+
 def build_reference() -> str | None:
-    """Builds the reference harness from the reference sources where they are present."""
-    if not os.path.isdir(REFERENCE_SRC):
-        return REF_LIB if os.path.exists(REF_LIB) and _loadable(REF_LIB) else None
-    subprocess.run(["make", "-s", "-f", "Makefile.ref", f"REF={REFERENCE_SRC}", "-j4"], cwd=ORACLE_DIR, check=True)
-    return REF_LIB
+    """Builds the reference harness (``_ref/libhcref.so``): from the checkout where there is one (and
+    then also writes the bundle), else from the bundle; None where neither is present."""
+    src = reference_source()
+    if src is not None:
+        _make(f"REF={src}")
+        _bundle(src)
+        return REF_LIB
+    if os.path.isfile(os.path.join(BUNDLE_DIR, "Block.cpp")):
+        args = (f"REF={BUNDLE_DIR}", f"BLOCK_CPP={os.path.join(BUNDLE_DIR, 'Block.cpp')}")
+        _make(*args)
+        if not _loadable(REF_LIB):  # a library built for another host came along with the bundle
+            _make("-B", *args)
+        return REF_LIB
+    return REF_LIB if os.path.exists(REF_LIB) and _loadable(REF_LIB) else None
 
 
 def _loadable(path: str) -> bool:
@@ -162,6 +210,26 @@ def mesh_many(runner, blocks: np.ndarray, heights: np.ndarray, nbr: np.ndarray, 
     fn = getattr(runner.lib, runner.prefix + "_mesh_many")
     q = fn(blocks.ctypes.data, heights.ctypes.data, nbr.ctypes.data, nbr.shape[0], threads, ctypes.byref(m))
     return int(q), int(m.value)
+
+
+def mesh_rows(runner, blocks: np.ndarray, heights: np.ndarray, nbr: np.ndarray, threads: int) -> list:
+    """The meshes of every row of the (n, 27) chunk-index table `nbr`, one list per row, computed on
+    `threads` threads (the foreign calls release the interpreter lock)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(row):
+        # each call sizes its own buffers (the runner's shared capacity hint only ever grows)
+        return runner.mesh_chunk([blocks[k] for k in row], [heights[k] for k in row])
+
+    with ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+        return list(ex.map(one, np.asarray(nbr)))
+
+
+def sample_positions(n: int, size: int, seed: int) -> np.ndarray:
+    """A seeded random sample of `size` of `n` batch positions, sorted; both bench arms and the
+    full-size parity test draw their samples this way."""
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, min(n, size), replace=False))
 
 
 def _bind_oracle_extras(lib):

@@ -7,7 +7,7 @@
 //   kMesh runner glue ........ client/src/ChunkMeshTask.cpp:41-122 (seed 49-87, BFS 89-111, mesh 113-122)
 //   window index ............. client/src/ChunkMeshTask.cpp:10-12
 //   light BFS ................ client/include/client/BlockLightAlgo.hpp:24-73 (Border = 14,
-//                              bound [-1,33)^3 from client/include/client/ChunkMeshTask.inl:181-184)
+//                              bound [-1,33)^3 from client/include/client/ChunkMeshTask.inl:53-56)
 //   mesher ................... client/include/client/BlockMeshAlgo.hpp:17-521
 //   loop/swizzle order ....... client/include/client/BlockAlgo.hpp:20-95 (YZX)
 //   vertex packing ........... client/include/client/BlockVertex.hpp:8-25
@@ -305,7 +305,7 @@ struct Mesher {
 					const hc_mesh_face *faces = r.static_faces + p.mesh_first;
 					uint32_t face_count = p.mesh_count;
 					if (p.mesh_kind == HC_MESH_FLOW) {
-						// fetch order of kLiquidFlowMesh (Liquid.hpp:406-415)
+						// fetch order of kLiquidFlowMesh (Liquid.hpp:291-300)
 						static const int kFetch[8][2] = {{-1, -1}, {0, -1}, {1, -1}, {-1, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
 						uint16_t nei[8];
 						for (int i = 0; i < 8; ++i)

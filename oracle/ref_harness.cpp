@@ -22,7 +22,7 @@ using namespace hc::client;
 
 namespace {
 
-// ChunkMeshTask.inl:181-184: the light algorithm of the kMesh runner.
+// ChunkMeshTask.inl:53-56: the light algorithm of the kMesh runner.
 using LightAlgo = BlockLightAlgo<BlockAlgoConfig<InnerPos1, BlockAlgoBound<InnerPos1>{-1, -1, -1, (InnerPos1)kChunkSize + 1,
                                                                                      (InnerPos1)kChunkSize + 1,
                                                                                      (InnerPos1)kChunkSize + 1}>,
