@@ -575,6 +575,19 @@ def serve_rates(ctx, rates, seconds, ctas):
     lib = hs.ChunkLibrary(16, 8, 16, seed=0x5E7E)
     rows = []
     names = {hs.REQ_EDIT: "edit", hs.REQ_FILL: "fill", hs.REQ_LOAD: "load", hs.REQ_UNLOAD: "unload"}
+    # warm-up (not reported): a short trace on a throwaway server, so that one-time costs of the
+    # process (the first launches of each kernel, first-use allocations) fall outside every rate
+    wl = hs.ServingWorkload(lib, seed=1)
+    init = wl.initial_loads()
+    reqs, times = wl.trace(rates[0], 0.3)
+    srv = hs.Server(ctx, wl.grid, wl.origin, pool_capacity=0, tick_us=1000, depth=3, max_edits_per_tick=16384,
+                    max_loads_per_tick=512, arena_quads=8 << 20, arena_meshes=1 << 16, ctas_per_chunk=ctas)
+    srv.submit(init)
+    srv.drain()
+    srv.start()
+    srv.replay(reqs, times)
+    srv.stop()
+    srv.close()
     for rate in rates:
         wl = hs.ServingWorkload(lib, seed=int(rate))
         init = wl.initial_loads()

@@ -636,7 +636,7 @@ hc_status hc_ctx_create(int device, hc_ctx **out) {
 		chk(cudaMalloc(&ctx->d_planes, 27 * (size_t)kPlaneStride * sizeof(uint32_t)), "planes");
 		chk(cudaMalloc(&ctx->d_cursor, 2 * sizeof(unsigned long long)), "cursor");
 		chk(cudaMalloc(&ctx->d_results, 8 * sizeof(uint32_t)), "results");
-		chk(cudaMalloc(&ctx->d_spill, (size_t)kSpillRecs * sizeof(uint2)), "record scratch");
+		chk(cudaMalloc(&ctx->d_spill, (size_t)kCtaScratch * sizeof(uint2)), "record and key scratch");
 		chk(cudaMallocHost(&ctx->h_results, 8 * sizeof(uint32_t)), "pinned results");
 	} while (0);
 	if (s != HC_OK) {
@@ -1092,7 +1092,7 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 		                     ? 1
 		                     : std::max(p->grid, std::max(p->cluster_grid[HC_VARIANT_CLUSTER2],
 		                                                  p->cluster_grid[HC_VARIANT_CLUSTER4]));
-		e = cudaMalloc(&p->d_spill, (size_t)ctas * kSpillRecs * sizeof(uint2));
+		e = cudaMalloc(&p->d_spill, (size_t)ctas * kCtaScratch * sizeof(uint2));
 	}
 	if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT) // the one-CTA persistent kernel skips blank chunks
 		e = cudaMalloc(&p->d_blank, n);
@@ -1551,7 +1551,7 @@ hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc,
 			e = cudaMemset(*p, 0, bytes > 0 ? bytes : 1);
 	};
 	A((void **)&w->d_slots, cells * sizeof(int32_t));
-	A((void **)&w->d_spill, (size_t)w->sms * kSpillRecs * sizeof(uint2));
+	A((void **)&w->d_spill, (size_t)w->sms * kCtaScratch * sizeof(uint2));
 	A((void **)&w->d_flags, cells * sizeof(uint32_t));
 	A((void **)&w->d_flood, (size_t)w->flood_words * sizeof(uint32_t));
 	A((void **)&w->d_stale, (size_t)pool->capacity * sizeof(uint32_t));

@@ -676,12 +676,22 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 		const int p = item & 255, part = (item >> 8) & 3, ks = item >> 10;
 		const int r0 = part == 2 ? (int)S.split_row[ks] : 0, r1 = part == 1 ? (int)S.split_row[ks] : 32;
 		const int lo = r0 > 0 ? r0 - 1 : 0;
-		const uint32_t N = plane_complex_one(S, p, lo, r0, r1, part == 2 ? S.split_side[ks] : nullptr);
+		const uint32_t V = plane_complex_one(S, p, lo, r0, r1, part == 2 ? S.split_side[ks] : nullptr);
 		uint32_t *mrow = S.u.masks[p][lane];
 		if (lane >= r0 && lane < r1)
 			mrow[1] = 0;
 		if (lane >= lo && (lane < r1 - 1 || (lane == 31 && r1 == 32)))
 			mrow[2] = 0;
+		// A lone face (no visible face left, right, above or below it in the plane) takes part in no
+		// equality: it is a quad of its own whatever its key, so it is not keyed here (the emission
+		// computes its light). The rows next to a row this warp does not resolve (the other half of
+		// a split plane) are keyed whole.
+		const uint32_t Vu1 = __shfl_up_sync(0xffffffffu, V, 1), Vd1 = __shfl_down_sync(0xffffffffu, V, 1);
+		const uint32_t Vup = lane == 0 ? 0u : Vu1, Vdn = lane == 31 ? 0u : Vd1;
+		const bool resolved_around = !(lane == r1 - 1 && r1 < 32) && !(lane == lo && lo > 0);
+		const uint32_t lone = resolved_around ? (V & ~(V << 1) & ~(V >> 1) & ~Vup & ~Vdn) : 0u;
+		const bool any_face = __any_sync(0xffffffffu, V != 0);
+		const uint32_t N = V & ~lone; // the faces keyed; every visible neighbour of one of them is one too
 		const uint32_t cnt = __popc(N);
 		uint32_t incl = cnt;
 #pragma unroll
@@ -721,8 +731,12 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 			const uint32_t Nu = __shfl_sync(0xffffffffu, N, u);
 			const int v = has ? nth_set_bit(Nu, k) : 0;
 			Key key{0, 0, 0};
-			if (has)
-				key = face_key(S, a, s, inv, u, v, nullptr, nullptr);
+			if (has) {
+				Light4 l;
+				key = face_key(S, a, s, inv, u, v, nullptr, &l);
+				if (S.keys) // kept for the emission of the quad this face may start
+					S.keys[p * 1024 + u * 32 + v] = pack_light4(l);
+			}
 			// right neighbour: next lane when (u, v + 1) is visible
 			const Key right = shfl_down_key(key);
 			const bool rv = has && v < 31 && ((Nu >> (v + 1)) & 1u);
@@ -747,7 +761,7 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 		}
 		__syncwarp();
 		if (part == 0) {
-			if (total != 0)
+			if (any_face)
 				plane_count_one(S, p);
 			continue;
 		}
@@ -823,11 +837,13 @@ __device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], G &&on_
 	}
 }
 
-// Quad record: plane, row, column, width-1, height-1, stream; then the quad's index among the
-// plane's quads (all streams) and among the plane's quads of its stream.
-__device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, int st, uint32_t li, uint32_t lk) {
+// Quad record: plane, row, column, width-1, height-1, stream, whether the first face's light key
+// is in the key scratch (it is not a lone face); then the quad's index among the plane's quads (all
+// streams) and among the plane's quads of its stream.
+__device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, int st, uint32_t li, uint32_t lk,
+                                             bool keyed = false) {
 	return make_uint2((uint32_t)p | ((uint32_t)u << 8) | ((uint32_t)v << 13) | ((uint32_t)(w - 1) << 18) |
-	                      ((uint32_t)(h - 1) << 23) | ((uint32_t)st << 28),
+	                      ((uint32_t)(h - 1) << 23) | ((uint32_t)st << 28) | ((uint32_t)keyed << 29),
 	                  li | (lk << 16));
 }
 
@@ -859,6 +875,9 @@ __device__ void plane_count_one(Smem &S, int p) {
 	const uint32_t(*m)[4] = S.u.masks[p];
 	const uint32_t rN = m[lane][0], rE = m[lane][1], rD = m[lane][2], rT = m[lane][3];
 	const uint32_t rDup = __shfl_up_sync(0xffffffffu, rD, 1);
+	// lone faces (no visible face beside, above or below): the key pass left their keys out
+	const uint32_t rNu = __shfl_up_sync(0xffffffffu, rN, 1), rNd = __shfl_down_sync(0xffffffffu, rN, 1);
+	const uint32_t rLone = rN & ~(rN << 1) & ~(rN >> 1) & ~(lane == 0 ? 0u : rNu) & ~(lane == 31 ? 0u : rNd);
 	const bool iso = rD == 0 && (lane == 0 || rDup == 0);
 	const uint32_t icont = rN & (rN << 1) & (rE << 1); // bit v continues the run of v - 1
 	const uint32_t istarts = iso ? (rN & ~icont) : 0u;
@@ -883,13 +902,15 @@ __device__ void plane_count_one(Smem &S, int p) {
 		const uint32_t cnt = __popc(starts), c1 = __popc(starts & tmask);
 		const uint32_t base = __shfl_sync(0xffffffffu, b, 0);
 		const uint32_t ex = __shfl_sync(0xffffffffu, iexcl, u); // isolated quads of the rows above u
+		const uint32_t lone_u = __shfl_sync(0xffffffffu, rLone, u);
 		if (is_start) {
 			const int st = (int)((tmask >> lane) & 1u);
 			const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
 			const uint32_t ex_all = ex & 0xffffu, ex_t = ex >> 16;
 			const uint32_t li = ex_all + b_all + __popc(starts & lt);
 			const uint32_t lk = (st ? ex_t + b_st[1] : ex_all - ex_t + b_st[0]) + __popc(same & lt);
-			put_record(S, base + __popc(starts & lt), quad_record(p, u, lane, w, h, st, li, lk));
+			const bool keyed = !((lone_u >> lane) & 1u);
+			put_record(S, base + __popc(starts & lt), quad_record(p, u, lane, w, h, st, li, lk, keyed));
 		}
 		if (lane == u)
 			mine = cnt | (c1 << 16);
@@ -909,7 +930,7 @@ __device__ void plane_count_one(Smem &S, int p) {
 		const int w = __ffs(~after); // cells from v to the end of its run
 		const int st = (int)((rT >> v) & 1u);
 		const uint32_t lk = st ? e_t + k_t : e_all - e_t + (k_all - k_t);
-		put_record(S, j + k_all, quad_record(p, lane, v, w, 1, st, e_all + k_all, lk));
+		put_record(S, j + k_all, quad_record(p, lane, v, w, 1, st, e_all + k_all, lk, !((rLone >> v) & 1u)));
 		++k_all;
 		k_t += (uint32_t)st;
 	}
@@ -923,14 +944,23 @@ __device__ void plane_count_one(Smem &S, int p) {
 // Writes quad (u, v, w, h) of plane p: stream st, stream index k, all-stream index g. Called by all
 // lanes of a warp; lanes without a quad (valid false) only take part in the box reduction.
 __device__ void emit_plane_quad(Smem &S, const Emit &E, bool valid, int p, int u, int v, int w, int h, int st, uint32_t k,
-                                uint32_t g) {
+                                uint32_t g, bool keyed = false) {
 	uint32_t mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
 	if (valid) {
 		const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
 		const bool uv_cycle = a != 2; // (U + 1) % 3 == V for the YZX swizzle (BlockMeshAlgo.hpp:384)
 		uint16_t t;
 		Light4 l;
-		face_key(S, a, s, inv, u, v, &t, &l);
+		if (keyed && S.keys) { // the key pass kept this face's light
+			int x, y, z;
+			to_xyz(a, s, u, v, x, y, z);
+			if (!inv)
+				(a == 0 ? x : (a == 1 ? y : z)) -= 1;
+			t = get_tex(S, x, y, z, 2 * a + inv);
+			l = unpack_light4(__ldcg(S.keys + p * 1024 + u * 32 + v));
+		} else {
+			face_key(S, a, s, inv, u, v, &t, &l);
+		}
 		int o[3], hv[3], wv[3];
 		to_xyz(a, s, u, v, o[0], o[1], o[2]);
 		to_xyz(a, 0, h, 0, hv[0], hv[1], hv[2]);
@@ -958,7 +988,7 @@ __device__ __forceinline__ void emit_record(Smem &S, const Emit &E, bool valid, 
 	const uint32_t li = r.y & 0xffffu, lk = r.y >> 16;
 	emit_plane_quad(S, E, valid, p, (int)((r.x >> 8) & 31u), (int)((r.x >> 13) & 31u), (int)((r.x >> 18) & 31u) + 1,
 	                (int)((r.x >> 23) & 31u) + 1, st, valid ? S.seg_base[st][1 + p] + lk : 0u,
-	                valid ? S.seg_base[2][1 + p] + li : 0u);
+	                valid ? S.seg_base[2][1 + p] + li : 0u, (r.x >> 29) & 1u);
 }
 
 // Emits the plane quads this CTA owns. Normally plane_count_one kept all their records; otherwise
@@ -1117,7 +1147,7 @@ struct Arena {
 	unsigned long long quad_cap;
 	unsigned int mesh_cap;
 	uint32_t *results;     // per batch position: opaque quads, transparent quads, first mesh, mesh count, status
-	uint2 *spill = nullptr; // kSpillRecs quad records per CTA of the grid (blockIdx.x), or null
+	uint2 *spill = nullptr; // kCtaScratch words per CTA of the grid (blockIdx.x): records, then keys; or null
 };
 
 enum : uint32_t { kChunkOk = 0, kChunkCapacity = 1 };
@@ -1143,8 +1173,10 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 	             // cluster, the relight's) order this before any CTA's plane phases
 		S.misc[tid < 4 ? kClaimComplex + tid : tid] = 0;
 	if (tid == 0) {
-		S.spill = A.spill ? A.spill + (size_t)blockIdx.x * kSpillRecs : nullptr;
-		S.spill_cap = A.spill ? kSpillRecs : 0u;
+		uint2 *const mine = A.spill ? A.spill + (size_t)blockIdx.x * kCtaScratch : nullptr;
+		S.spill = mine;
+		S.spill_cap = mine ? kSpillRecs : 0u;
+		S.keys = mine ? mine + kSpillRecs : nullptr;
 	}
 	bool has_custom;
 	const bool blank = stage_classes(S, T, has_custom);
