@@ -389,7 +389,7 @@ def measure_batch(args, ctx, workload, rank, world, local, *, plain=True, e2e=Tr
                 "traffic": traffic["bytes"] if traffic else None,
                 "traffic_capture": traffic["capture"] if traffic else None,
                 "peak_source": f"{peak_kind} ({'MEASURED_PEAKS.json hbm_gbs' if peak_kind == 'measured' else 'fallback'})",
-                "kernel": "k_mesh_batch" if variant < 2 else "k_mesh_cluster", "kernel_ms": mesh_ms,
+                "kernel": "k_mesh_cluster" if variant in (2, 3) else "k_mesh_batch", "kernel_ms": mesh_ms,
                 "stage_ms": {"planes": float(stages[0]), "light_pass": float(stages[1]), "mesh": float(stages[2])},
                 "algorithmic_bytes_per_launch": algo_bytes,
                 "step_frac": algo_bytes / (ms_step / 1e3) / 1e9 / peak,
@@ -499,7 +499,7 @@ def measure_batch(args, ctx, workload, rank, world, local, *, plain=True, e2e=Tr
            "batched_vs_plain": (value / world / plain_value) if plain_value else None,
            "autotuned_variant": variant_name, "variant_ms": dict(zip(batch.VARIANTS, variant_ms)),
            "roofline": roofline, "e2e": e2e_line, "cpu_baseline": cpu_line, "parity_vs_cpu_sample": parity,
-           "gpu_launches": args.steps * (18 if variant == 0 else (3 if variant == 1 else 2)),
+           "gpu_launches": args.steps * batch.launches_per_run(variant),
            "clocks": clk.summary(),
            "l2": f"inputs larger than L2: pool {w.n_chunks * 66560 / 1e6:.0f} MB, output {(44 * quads) / 1e6:.0f} MB "
                  f"per step"}

@@ -23,7 +23,17 @@ def variant_mode(v: int) -> int:
 
 
 VARIANTS = ("light pass, one CTA per chunk", "window relight, one CTA per chunk", "window relight, 2-CTA clusters",
-            "window relight, 4-CTA clusters")
+            "window relight, 4-CTA clusters", "light pass, 2 chunks per claim", "light pass, 4 chunks per claim",
+            "light pass, no global record scratch (windowed emission)")
+LIGHT_PASS_VARIANTS = (0, 4, 5, 6)
+
+
+def launches_per_run(v: int) -> int:
+    """Kernels one run of persistent variant v launches: plane refresh, blank test (one CTA per
+    chunk), 15 light levels (light-pass variants) and the mesher."""
+    return 18 if v in LIGHT_PASS_VARIANTS else (3 if v == 1 else 2)
+
+
 RESULT_OK, RESULT_ARENA_FULL, RESULT_BAD_SLOT = 0, 1, 2
 
 
@@ -177,7 +187,7 @@ class BatchPlan:
     def variant(self):
         """(variant index, its description, ms per variant as timed by the autotuner)."""
         v = ctypes.c_int()
-        ms = np.zeros(4, np.float32)
+        ms = np.zeros(len(VARIANTS), np.float32)
         self.lib.hc_batch_plan_variant(self.handle, ctypes.byref(v), ms.ctypes.data)
         return v.value, VARIANTS[v.value], [float(x) for x in ms]
 

@@ -53,10 +53,6 @@ enum : uint32_t {
 // = 202,752; beyond the scratch the emission merges the planes again in windows).
 constexpr int kQuadBuf = 4096;
 constexpr uint32_t kSpillRecs = 1u << 17;
-// After the records, each CTA's scratch holds the light key of every keyed face (8 bytes), at
-// plane * 1024 + row * 32 + column, so that the emission reads it instead of computing it again.
-constexpr uint32_t kKeySlots = 198u * 1024u;
-constexpr uint32_t kCtaScratch = kSpillRecs + kKeySlots; // uint2 words per CTA
 
 // One block class: a distinct property row of the registry (65,536 raw values map onto < 256).
 struct DevClass {
@@ -156,7 +152,6 @@ struct Smem {
 	uint32_t trig[2][kMaxMeshesPerStream];
 	uint32_t misc[16];
 	uint2 *spill;       // this CTA's quad records past kQuadBuf (global scratch), or null
-	uint2 *keys;        // this CTA's face light keys by plane and cell (global scratch), or null
 	uint32_t spill_cap; // records it holds
 	uint8_t plane_owner[kPlanes]; // cluster form, in CTA 0: the CTA that took each face plane
 	uint8_t mine[kPlanes];        // the face planes this CTA took, in the order it took them
@@ -324,18 +319,6 @@ __device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
 		r.torch |= (q >> 16) << (8 * v);
 	}
 	return r;
-}
-
-// A Light4 in eight bytes: the sun bytes as they are; the torch values (each at most 60) in six
-// bits each, then the AO byte.
-__device__ __forceinline__ uint2 pack_light4(const Light4 &l) {
-	const uint32_t t = l.torch;
-	const uint32_t t6 = (t & 0x3fu) | ((t >> 2) & 0xfc0u) | ((t >> 4) & 0x3f000u) | ((t >> 6) & 0xfc0000u);
-	return make_uint2(l.sun, t6 | (l.ao << 24));
-}
-__device__ __forceinline__ Light4 unpack_light4(uint2 k) {
-	const uint32_t t6 = k.y & 0xffffffu;
-	return Light4{k.x, (t6 & 0x3fu) | ((t6 & 0xfc0u) << 2) | ((t6 & 0x3f000u) << 4) | ((t6 & 0xfc0000u) << 6), k.y >> 24};
 }
 
 __device__ __forceinline__ uint32_t l4_get(uint32_t packed, int i) { return (packed >> (8 * i)) & 0xffu; }

@@ -200,23 +200,26 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_mesh_batch(const uint16_t *pool_blocks, const int8_t *pool_heights, const uint32_t *pool_planes, uint32_t pool_cap,
                  const int32_t *nbr, uint32_t n, const uint32_t *n_dev, unsigned int *work, unsigned int *failed,
                  DevTables T, Arena A, const uint32_t *levels, const uint32_t *edges, const int32_t *nbr_local,
-                 const uint32_t *lflags, const uint8_t *item_blank) {
+                 const uint32_t *lflags, const uint8_t *item_blank, uint32_t claim) {
 	Smem &S = smem();
 	__shared__ uint32_t s_next;
 	if (n_dev) // the batch length is known on the device only (a world remesh)
 		n = *n_dev;
 	if (threadIdx.x == 0)
-		s_next = atomicAdd(work, 1u);
+		s_next = atomicAdd(work, claim);
 	__syncthreads();
-	uint32_t item = s_next;
+	uint32_t item = s_next, left = claim; // a claim takes `claim` consecutive chunks
 	for (;;) {
 		if (item >= n)
 			break;
 		__syncthreads(); // everyone has read s_next
-		if (threadIdx.x == 0)
-			s_next = atomicAdd(work, 1u);
-		__syncthreads();
-		const uint32_t next = s_next;
+		uint32_t next = item + 1;
+		if (left == 1) {
+			if (threadIdx.x == 0)
+				s_next = atomicAdd(work, claim);
+			__syncthreads();
+			next = s_next;
+		}
 		if (next < n && !(item_blank && item_blank[next]))
 			prefetch_item(pool_blocks, pool_planes, pool_cap, nbr, next, levels, nbr_local);
 		if (item_blank && item_blank[item]) { // no quad: the results a blank chunk gets
@@ -231,6 +234,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 			bad_item(A, item, failed);
 		}
 		__syncthreads();
+		left = left == 1 ? claim : left - 1;
 		item = next;
 	}
 }
@@ -355,8 +359,8 @@ struct hc_batch_plan {
 	int mode = HC_BATCH_PERSISTENT;
 	int grid = 0;
 	int variant = HC_VARIANT_LIGHT_PASS;
-	float variant_ms[4] = {0, 0, 0, 0};
-	int cluster_grid[4] = {0, 0, 0, 0}; // persistent grid of the cluster variants
+	float variant_ms[HC_VARIANT_COUNT] = {};
+	int cluster_grid[HC_VARIANT_COUNT] = {}; // persistent grid of the cluster variants
 	int32_t *d_slots = nullptr;            // distinct valid slots the batch reads (their planes are refreshed)
 	uint32_t n_slots = 0;
 	// batch light pass (persistent form): the distinct slots are the batch's chunks 0..n_slots-1
@@ -636,7 +640,7 @@ hc_status hc_ctx_create(int device, hc_ctx **out) {
 		chk(cudaMalloc(&ctx->d_planes, 27 * (size_t)kPlaneStride * sizeof(uint32_t)), "planes");
 		chk(cudaMalloc(&ctx->d_cursor, 2 * sizeof(unsigned long long)), "cursor");
 		chk(cudaMalloc(&ctx->d_results, 8 * sizeof(uint32_t)), "results");
-		chk(cudaMalloc(&ctx->d_spill, (size_t)kCtaScratch * sizeof(uint2)), "record and key scratch");
+		chk(cudaMalloc(&ctx->d_spill, (size_t)kSpillRecs * sizeof(uint2)), "record scratch");
 		chk(cudaMallocHost(&ctx->h_results, 8 * sizeof(uint32_t)), "pinned results");
 	} while (0);
 	if (s != HC_OK) {
@@ -864,16 +868,26 @@ hc_status hc_pool_download(hc_pool *pool, uint32_t first, uint32_t count, uint16
 
 namespace {
 
+// The knobs of persistent variant v (include/hc_gb300.h, HC_VARIANT_*).
+int variant_cluster(int v) { return v == HC_VARIANT_CLUSTER2 ? 2 : (v == HC_VARIANT_CLUSTER4 ? 4 : 0); }
+bool variant_light_pass(int v) { return v != HC_VARIANT_WINDOW && !variant_cluster(v); }
+uint32_t variant_claim(int v) { return v == HC_VARIANT_CLAIM2 ? 2u : (v == HC_VARIANT_CLAIM4 ? 4u : 1u); }
+// quad records past shared memory are dropped and the emission merges again in windows
+bool variant_no_scratch(int v) { return v == HC_VARIANT_NO_SCRATCH; }
+
 Arena plan_arena(const hc_batch_plan *p) {
-	return Arena{reinterpret_cast<uint2 *>(p->arena.vertices),
-	             p->arena.indices,
-	             p->arena.meshes,
-	             p->d_state,
-	             reinterpret_cast<unsigned int *>(p->d_state + 1),
-	             p->arena.quad_capacity,
-	             p->arena.mesh_capacity,
-	             p->arena.results,
-	             p->d_spill};
+	Arena A{reinterpret_cast<uint2 *>(p->arena.vertices),
+	        p->arena.indices,
+	        p->arena.meshes,
+	        p->d_state,
+	        reinterpret_cast<unsigned int *>(p->d_state + 1),
+	        p->arena.quad_capacity,
+	        p->arena.mesh_capacity,
+	        p->arena.results,
+	        p->d_spill};
+	if (p->mode == HC_BATCH_PERSISTENT && variant_no_scratch(p->variant))
+		A.spill = nullptr;
+	return A;
 }
 
 cudaLaunchConfig_t cluster_config(dim3 grid, size_t smem, cudaStream_t st, cudaLaunchAttribute *attr, int csize) {
@@ -980,13 +994,13 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		                                     p->pool->d_planes);
 		HC_CUDA(ctx, cudaGetLastError());
 	}
-	if (p->d_blank && p->n_slots && p->variant < HC_VARIANT_CLUSTER2) {
+	if (p->d_blank && p->n_slots && !variant_cluster(p->variant)) {
 		k_blank_items<<<(p->n + 7) / 8, 256, 0, st>>>(p->pool->d_planes, p->pool->capacity, p->nbr, p->n, p->d_blank);
 		HC_CUDA(ctx, cudaGetLastError());
 	}
 	if ((s = stage_mark(p, 1, st)) != HC_OK)
 		return s;
-	const bool light_pass = p->variant == HC_VARIANT_LIGHT_PASS && p->d_levels;
+	const bool light_pass = variant_light_pass(p->variant) && p->d_levels;
 	if (light_pass) {
 		const LightPass L{p->d_slots,  p->d_nb6,   p->pool->d_planes, p->pool->d_blocks, p->d_levels,
 		                  p->d_edges, p->d_lflags, p->d_lflags + 2 * (size_t)p->n_slots, p->n_slots};
@@ -1001,8 +1015,8 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 	const Arena A = plan_arena(p);
 	unsigned int *work = reinterpret_cast<unsigned int *>(p->d_state + 2);
 	unsigned int *failed = reinterpret_cast<unsigned int *>(p->d_state + 3);
-	if (p->mode == HC_BATCH_PERSISTENT && p->variant >= HC_VARIANT_CLUSTER2) {
-		const int csize = p->variant == HC_VARIANT_CLUSTER2 ? 2 : 4;
+	if (p->mode == HC_BATCH_PERSISTENT && variant_cluster(p->variant)) {
+		const int csize = variant_cluster(p->variant);
 		cudaLaunchAttribute attr[1];
 		cudaLaunchConfig_t cfg = cluster_config(dim3(p->cluster_grid[p->variant]), ctx->smem_bytes, st, attr, csize);
 		HC_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_mesh_cluster, (const uint16_t *)p->pool->d_blocks,
@@ -1014,7 +1028,8 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		k_mesh_batch<<<p->grid, kThreads, ctx->smem_bytes, st>>>(
 		    p->pool->d_blocks, p->pool->d_heights, p->pool->d_planes, p->pool->capacity, p->nbr, p->n, nullptr, work,
 		    failed, tables(ctx), A, light_pass ? p->d_levels : nullptr, light_pass ? p->d_edges : nullptr,
-		    light_pass ? p->d_nbr_local : nullptr, light_pass ? p->d_lflags : nullptr, p->d_blank);
+		    light_pass ? p->d_nbr_local : nullptr, light_pass ? p->d_lflags : nullptr, p->d_blank,
+		    variant_claim(p->variant));
 		HC_CUDA(ctx, cudaGetLastError());
 	} else {
 		for (uint32_t i = 0; i < p->n; ++i) {
@@ -1034,11 +1049,11 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 	    !arena->meshes || !arena->results)
 		return HC_ERR_INVALID_ARG;
 	if (mode != HC_BATCH_PERSISTENT && mode != HC_BATCH_PER_CHUNK && mode != HC_BATCH_AUTO &&
-	    !(mode >= HC_BATCH_VARIANT(HC_VARIANT_LIGHT_PASS) && mode <= HC_BATCH_VARIANT(HC_VARIANT_CLUSTER4)))
+	    !(mode >= HC_BATCH_VARIANT(0) && mode < HC_BATCH_VARIANT(HC_VARIANT_COUNT)))
 		return fail(ctx, HC_ERR_INVALID_ARG, "unknown batch mode");
 	const bool autotune = mode == HC_BATCH_AUTO;
-	// the persistent variants to build: the light pass, one pinned variant, or (autotuning) all four
-	int first = HC_VARIANT_LIGHT_PASS, last = autotune ? HC_VARIANT_CLUSTER4 : HC_VARIANT_LIGHT_PASS;
+	// the persistent variants to build: the light pass, one pinned variant, or (autotuning) all of them
+	int first = HC_VARIANT_LIGHT_PASS, last = autotune ? HC_VARIANT_COUNT - 1 : HC_VARIANT_LIGHT_PASS;
 	if (mode >= HC_BATCH_VARIANT(0))
 		first = last = mode - HC_BATCH_VARIANT(0);
 	if (autotune || mode >= HC_BATCH_VARIANT(0))
@@ -1092,7 +1107,7 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
 		                     ? 1
 		                     : std::max(p->grid, std::max(p->cluster_grid[HC_VARIANT_CLUSTER2],
 		                                                  p->cluster_grid[HC_VARIANT_CLUSTER4]));
-		e = cudaMalloc(&p->d_spill, (size_t)ctas * kCtaScratch * sizeof(uint2));
+		e = cudaMalloc(&p->d_spill, (size_t)ctas * kSpillRecs * sizeof(uint2));
 	}
 	if (e == cudaSuccess && mode == HC_BATCH_PERSISTENT) // the one-CTA persistent kernel skips blank chunks
 		e = cudaMalloc(&p->d_blank, n);
@@ -1178,13 +1193,13 @@ hc_status hc_batch_plan_stage_ms(hc_batch_plan *plan, float ms[3]) {
 	return HC_OK;
 }
 
-hc_status hc_batch_plan_variant(const hc_batch_plan *plan, int *variant, float ms[4]) {
+hc_status hc_batch_plan_variant(const hc_batch_plan *plan, int *variant, float ms[HC_VARIANT_COUNT]) {
 	if (!plan)
 		return HC_ERR_INVALID_ARG;
 	if (variant)
 		*variant = plan->variant;
 	if (ms)
-		for (int v = 0; v < 4; ++v)
+		for (int v = 0; v < HC_VARIANT_COUNT; ++v)
 			ms[v] = plan->variant_ms[v];
 	return HC_OK;
 }
@@ -1405,7 +1420,7 @@ hc_status world_enqueue_remesh(hc_world *w, const hc_batch_arena *arena, cudaStr
 	} else {
 		k_mesh_batch<<<w->sms, kThreads, ctx->smem_bytes, st>>>(
 		    w->pool->d_blocks, w->pool->d_heights, w->pool->d_planes, w->pool->capacity, w->d_nbr, 0u,
-		    w->d_counts + kCountRemesh, work, failed, tables(ctx), A, nullptr, nullptr, nullptr, nullptr, nullptr);
+		    w->d_counts + kCountRemesh, work, failed, tables(ctx), A, nullptr, nullptr, nullptr, nullptr, nullptr, 1u);
 	}
 	HC_CUDA(ctx, cudaGetLastError());
 	k_requeue<<<list_grid(w), 256, 0, st>>>(W, w->d_list, A.results);
@@ -1551,7 +1566,7 @@ hc_status hc_world_create(hc_ctx *ctx, hc_pool *pool, const hc_world_desc *desc,
 			e = cudaMemset(*p, 0, bytes > 0 ? bytes : 1);
 	};
 	A((void **)&w->d_slots, cells * sizeof(int32_t));
-	A((void **)&w->d_spill, (size_t)w->sms * kCtaScratch * sizeof(uint2));
+	A((void **)&w->d_spill, (size_t)w->sms * kSpillRecs * sizeof(uint2));
 	A((void **)&w->d_flags, cells * sizeof(uint32_t));
 	A((void **)&w->d_flood, (size_t)w->flood_words * sizeof(uint32_t));
 	A((void **)&w->d_stale, (size_t)pool->capacity * sizeof(uint32_t));
@@ -1893,7 +1908,7 @@ extern "C" hc_status hc_mesh_batch_noalloc(const uint16_t *pool_blocks, const in
 		        results};
 		k_mesh_batch<<<D.sms, kThreads, sizeof(Smem), st>>>(pool_blocks, pool_heights, nullptr, pool_capacity, neighbours,
 		                                                     n, nullptr, state + 4, state + 5, DevTables{D.class_of, D.classes}, A,
-		                                                     nullptr, nullptr, nullptr, nullptr, nullptr);
+		                                                     nullptr, nullptr, nullptr, nullptr, nullptr, 1u);
 		e = cudaGetLastError();
 	}
 	uint32_t host_state[kNoAllocStateWords];

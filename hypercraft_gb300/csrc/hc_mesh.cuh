@@ -107,28 +107,54 @@ __device__ __forceinline__ void aabb_add(Smem &S, int st, uint32_t m, const uint
 	atomicMax(bb + 3, mx[0]), atomicMax(bb + 4, mx[1]), atomicMax(bb + 5, mx[2]);
 }
 
-// The same for the quads of a whole warp (all lanes call it; `valid` lanes carry a quad): the quads
-// of the first valid lane's mesh are reduced over the full warp first, so a mesh's box takes six
-// atomics per warp instead of six per quad; lanes of another mesh add theirs one by one.
-__device__ __forceinline__ void aabb_add_warp(Smem &S, bool valid, int st, uint32_t m, const uint32_t mn[3],
-                                              const uint32_t mx[3]) {
-	const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
-	if (!vmask)
+// A warp's running box of one mesh (key = stream << 16 | mesh; every lane holds the box of its own
+// quads of that mesh): the emission grows it quad by quad in registers and adds it to the mesh's
+// box in shared memory (a warp reduction and six atomics) only when the warp moves on to another
+// mesh, and once at the end, instead of once per round of 32 quads.
+struct BoxAcc {
+	uint32_t key = 0xffffffffu;
+	uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0u, 0u, 0u};
+};
+
+// Adds the running box to its mesh's box (all lanes call it).
+__device__ __forceinline__ void box_flush(Smem &S, BoxAcc &b) {
+	if (b.key == 0xffffffffu)
 		return;
-	const int leader = __ffs(vmask) - 1;
-	const uint32_t key = ((uint32_t)st << 16) | m;
-	const uint32_t lkey = __shfl_sync(0xffffffffu, key, leader);
-	const bool same = valid && key == lkey;
 	uint32_t r[6];
 #pragma unroll
 	for (int c = 0; c < 3; ++c) {
-		r[c] = __reduce_min_sync(0xffffffffu, same ? mn[c] : 0xffffffffu);
-		r[3 + c] = __reduce_max_sync(0xffffffffu, same ? mx[c] : 0u);
+		r[c] = __reduce_min_sync(0xffffffffu, b.mn[c]);
+		r[3 + c] = __reduce_max_sync(0xffffffffu, b.mx[c]);
+		b.mn[c] = 0xffffffffu, b.mx[c] = 0u;
 	}
-	if ((int)(threadIdx.x & 31) == leader)
-		aabb_add(S, (int)(lkey >> 16), lkey & 0xffffu, r, r + 3);
-	if (valid && !same)
+	if ((threadIdx.x & 31) == 0)
+		aabb_add(S, (int)(b.key >> 16), b.key & 0xffffu, r, r + 3);
+	b.key = 0xffffffffu;
+}
+
+// Grows the boxes by one round of quads (all lanes call it; `valid` lanes carry a quad of mesh
+// (st, m) spanning [mn, mx]). The quads of the first valid lane's mesh go into the running box; a
+// lane of another mesh (a round that crosses a mesh boundary) adds its quad directly.
+__device__ __forceinline__ void box_add_warp(Smem &S, BoxAcc &b, bool valid, int st, uint32_t m, const uint32_t mn[3],
+                                             const uint32_t mx[3]) {
+	const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+	if (!vmask)
+		return;
+	const uint32_t key = ((uint32_t)st << 16) | m;
+	const uint32_t lkey = __shfl_sync(0xffffffffu, key, __ffs(vmask) - 1);
+	if (lkey != b.key) {
+		box_flush(S, b);
+		b.key = lkey;
+	}
+	if (valid && key == lkey) {
+#pragma unroll
+		for (int c = 0; c < 3; ++c) {
+			b.mn[c] = min(b.mn[c], mn[c]);
+			b.mx[c] = max(b.mx[c], mx[c]);
+		}
+	} else if (valid) {
 		aabb_add(S, st, m, mn, mx);
+	}
 }
 
 // Writes quad k of stream st (all-stream index g): 4 vertices, 6 indices, and the trigger of the
@@ -211,14 +237,13 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 		asm volatile("cp.async.commit_group;" ::: "memory");
 		for (int i = threadIdx.x; i < 256; i += kThreads)
 			S.classes[i] = T.classes[i];
-		// With the batch light pass's level planes the light bytes are decoded now, their loads
-		// overlapping the copies; the class ids then go into the high bytes of the cells alone.
-		// Otherwise the whole cell is written (light 0 for the relight to raise).
+		// With the batch light pass's level planes, each row's light is decoded after the row bits
+		// below (its loads overlapping the copies still in flight) and written together with the
+		// row's class ids as whole cells; otherwise the class ids go in with light 0, for the
+		// relight to raise.
 		const bool lit = S.lvl[26] != nullptr;
 		uint8_t *const hi = reinterpret_cast<uint8_t *>(S.cell) + 1;
-		if (lit)
-			light_from_levels(S);
-		// Meanwhile, one thread per row of [-1, 32]^2: the opaque-cube and blank bits of the row from
+		// First, one thread per row of [-1, 32]^2: the opaque-cube and blank bits of the row from
 		// its chunk's planes with the x = -1 and x = 32 bits from the x neighbours' (bit x + 1), and
 		// the class ids of the row's two edge cells.
 		for (int row = threadIdx.x; row < kRows; row += kThreads) {
@@ -238,10 +263,37 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 				S.cell[row * kCls + kCls - 1] = (uint16_t)(e1 << 8);
 			}
 		}
+		// the light of each row item is decoded now (its level-plane loads overlapping the copies still in flight)
+		// and kept in registers until the row's class ids have arrived; edge pieces are written now
+		constexpr int kLightItems = kLt * kLt + 2 * kLt * 3;
+		static_assert(kLightItems <= 2 * kThreads, "two light items per thread at most");
+		uint64_t lrow[2][4];
+		bool has_row[2] = {false, false};
+		if (lit) {
+#pragma unroll
+			for (int k = 0; k < 2; ++k) { // both items' level loads in flight together
+				const int it = threadIdx.x + k * kThreads;
+				if (it < kLightItems)
+					has_row[k] = light_item(S, it, lrow[k]);
+			}
+		}
 		asm volatile("cp.async.wait_group 0;" ::: "memory");
 		__syncthreads();
-		// class ids of the cells x in [0, 32) of every row, from the copies; one warp per row, lanes
-		// over x
+		if (lit) { // light and class id of the cells x in [0, 32) of each row item, as whole cells
+#pragma unroll
+			for (int k = 0; k < 2; ++k) {
+				if (!has_row[k])
+					continue;
+				const int row = threadIdx.x + k * kThreads, y = row / kCls - 1, z = row % kCls - 1;
+				const bool inner = (unsigned)y < (unsigned)kChunk && (unsigned)z < (unsigned)kChunk;
+				const int a = y < 0 ? z + 1 : (y >= kChunk ? 35 + z : 68 + 2 * y + (z >= kChunk)); // apron row
+				write_row_cells(S, row, lrow[k], own + (inner ? (y * kChunk + z) * kChunk : 32768 + 32 * a));
+			}
+			__syncthreads();
+			return false;
+		}
+		// without light-pass levels: class ids of the cells x in [0, 32) of every row, from the copies
+		// (light 0 for the relight to raise); one warp per row, lanes over x
 		for (int row0 = warp * kBatch; row0 < kRows; row0 += kWarps * kBatch) {
 			uint8_t c[kBatch];
 #pragma unroll
@@ -255,10 +307,7 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 			for (int j = 0; j < kBatch; ++j) {
 				if (row0 + j >= kRows) // the same for the whole warp
 					break;
-				if (lit)
-					hi[2 * ((row0 + j) * kCls + lane + 1)] = c[j];
-				else
-					S.cell[(row0 + j) * kCls + lane + 1] = (uint16_t)(c[j] << 8);
+				S.cell[(row0 + j) * kCls + lane + 1] = (uint16_t)(c[j] << 8);
 			}
 		}
 		__syncthreads();
@@ -664,14 +713,108 @@ __device__ __forceinline__ int claim_item(Smem &S, const Split &sp, int live, in
 
 __device__ void plane_count_one(Smem &S, int p);
 
+// Keyed faces of a plane's rows (lane = row): the visible words V with the lone faces left out.
+// A lone face (no visible face left, right, above or below it in the plane) takes part in no
+// equality: it is a quad of its own whatever its key, so it is not keyed (the emission computes its
+// light). Rows next to a row the calling warp does not resolve (the other half of a split plane,
+// outside [lo, r1)) are keyed whole. Every visible neighbour of a keyed face is keyed too.
+__device__ __forceinline__ uint32_t keyed_faces(uint32_t V, int lo, int r1) {
+	const int lane = threadIdx.x & 31;
+	const uint32_t Vu1 = __shfl_up_sync(0xffffffffu, V, 1), Vd1 = __shfl_down_sync(0xffffffffu, V, 1);
+	const uint32_t Vup = lane == 0 ? 0u : Vu1, Vdn = lane == 31 ? 0u : Vd1;
+	const bool resolved_around = !(lane == r1 - 1 && r1 < 32) && !(lane == lo && lo > 0);
+	const uint32_t lone = resolved_around ? (V & ~(V << 1) & ~(V >> 1) & ~Vup & ~Vdn) : 0u;
+	return V & ~lone;
+}
+
+// Inclusive warp scan (lane = row) of a row count.
+__device__ __forceinline__ uint32_t row_scan(uint32_t cnt) {
+	const int lane = threadIdx.x & 31;
+	uint32_t incl = cnt;
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+		if (lane >= d)
+			incl += o;
+	}
+	return incl;
+}
+
+// Small whole planes (at most 32 keyed faces each) are keyed together: a group of up to four such
+// planes fills one warp's lanes, so that the light of a sparse plane's faces is not computed by a
+// warp that is mostly idle. kGroupPlanes planes at most; the group is packed in two words per warp.
+constexpr int kGroupPlanes = 4;
+struct PlaneGroup {
+	uint32_t planes = 0; // plane ids, 8 bits each
+	uint32_t bases = 0;  // first lane of each plane, 8 bits each
+	int n = 0;           // planes in the group
+	uint32_t total = 0;  // lanes used
+};
+
+// Keys the faces of every plane of the group in one batch (each plane's faces fit in it whole, so
+// a face's right and upper neighbours are in the same batch), sets their equal-right and
+// equal-below bits, then merges and counts each plane. Empties the group.
+__device__ void key_group(Smem &S, PlaneGroup &G) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	if (G.n == 0)
+		return;
+	int my_p = 0, my_u = 0, my_v = 0, my_up = -1; // this lane's face, and the lane of its upper neighbour
+	uint32_t my_Nu = 0;
+	for (int g = 0; g < G.n; ++g) { // warp-uniform
+		const int p = (int)((G.planes >> (8 * g)) & 255u);
+		const uint32_t base = (G.bases >> (8 * g)) & 255u;
+		const uint32_t end = g + 1 < G.n ? (G.bases >> (8 * (g + 1))) & 255u : G.total;
+		const uint32_t N = keyed_faces(S.u.masks[p][lane][0], 0, 32);
+		const uint32_t cnt = __popc(N), incl = row_scan(cnt), start = incl - cnt;
+		// rows holding faces record themselves where their faces start (distinct lanes)
+		const uint32_t M = __reduce_or_sync(0xffffffffu, cnt ? 1u << start : 0u);
+		if (cnt)
+			S.row_of[warp][start] = (uint8_t)lane;
+		__syncwarp();
+		const bool mine = lane >= (int)base && lane < (int)end;
+		const uint32_t f = mine ? lane - base : 0u; // face index in the plane
+		const int u = mine ? S.row_of[warp][31 - __clz(M & (f == 31 ? 0xffffffffu : ((2u << f) - 1u)))] : 0;
+		__syncwarp();
+		const uint32_t su = __shfl_sync(0xffffffffu, start, u), Nu = __shfl_sync(0xffffffffu, N, u);
+		const uint32_t Nup = __shfl_sync(0xffffffffu, N, (u + 31) & 31), sup = __shfl_sync(0xffffffffu, start, (u + 31) & 31);
+		if (mine) {
+			const int v = nth_set_bit(Nu, f - su);
+			my_p = p, my_u = u, my_v = v, my_Nu = Nu;
+			my_up = u > 0 && ((Nup >> v) & 1u) ? (int)(base + sup + __popc(Nup & ((1u << v) - 1u))) : -1;
+		}
+	}
+	const bool has = lane < (int)G.total;
+	Key key{0, 0, 0};
+	if (has) {
+		const int a = my_p / 66, s = (my_p % 66) >> 1, inv = my_p & 1;
+		key = face_key(S, a, s, inv, my_u, my_v, nullptr, nullptr);
+	}
+	// right neighbour: the next lane when (u, v + 1) is visible (then it is keyed, in the same plane)
+	const Key right = shfl_down_key(key);
+	if (has && my_v < 31 && ((my_Nu >> (my_v + 1)) & 1u) && key_eq(key, right))
+		atomicOr(&S.u.masks[my_p][my_u][1], 1u << my_v);
+	// upper neighbour (u - 1, v)
+	const int src = my_up < 0 ? lane : my_up;
+	const Key up{__shfl_sync(0xffffffffu, key.tex_ao, src), __shfl_sync(0xffffffffu, key.sun, src),
+	             __shfl_sync(0xffffffffu, key.torch, src)};
+	if (has && my_up >= 0 && key_eq(key, up))
+		atomicOr(&S.u.masks[my_p][my_u - 1][2], 1u << my_v);
+	__syncwarp();
+	for (int g = 0; g < G.n; ++g)
+		plane_count_one(S, (int)((G.planes >> (8 * g)) & 255u));
+	G = PlaneGroup{};
+}
+
 // Pass 2 (after the relight): equal-to-right and equal-to-below masks of every plane, each plane
 // then merged and counted by the warp that built its masks (no block barrier in between). The visible
 // faces of a plane are taken in batches of whole rows (at most 32 faces), one face per lane, so
 // the light keys are computed by full warps; a face's right neighbour is the next lane and its
 // upper neighbour sits in this batch or in the previous one. A half plane keys rows [lo, r1) and
 // writes the equal-right bits of rows [r0, r1) and the equal-below bits of rows [lo, r1 - 1).
+// Whole planes with at most 32 keyed faces go into the warp's plane group instead (key_group).
 __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	PlaneGroup G;
 	for (int item = claim_item(S, sp, live, nsplit); (item & 255) < kPlanes; item = claim_item(S, sp, live, nsplit)) {
 		const int p = item & 255, part = (item >> 8) & 3, ks = item >> 10;
 		const int r0 = part == 2 ? (int)S.split_row[ks] : 0, r1 = part == 1 ? (int)S.split_row[ks] : 32;
@@ -682,27 +825,27 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 			mrow[1] = 0;
 		if (lane >= lo && (lane < r1 - 1 || (lane == 31 && r1 == 32)))
 			mrow[2] = 0;
-		// A lone face (no visible face left, right, above or below it in the plane) takes part in no
-		// equality: it is a quad of its own whatever its key, so it is not keyed here (the emission
-		// computes its light). The rows next to a row this warp does not resolve (the other half of
-		// a split plane) are keyed whole.
-		const uint32_t Vu1 = __shfl_up_sync(0xffffffffu, V, 1), Vd1 = __shfl_down_sync(0xffffffffu, V, 1);
-		const uint32_t Vup = lane == 0 ? 0u : Vu1, Vdn = lane == 31 ? 0u : Vd1;
-		const bool resolved_around = !(lane == r1 - 1 && r1 < 32) && !(lane == lo && lo > 0);
-		const uint32_t lone = resolved_around ? (V & ~(V << 1) & ~(V >> 1) & ~Vup & ~Vdn) : 0u;
 		const bool any_face = __any_sync(0xffffffffu, V != 0);
-		const uint32_t N = V & ~lone; // the faces keyed; every visible neighbour of one of them is one too
+		const uint32_t N = keyed_faces(V, lo, r1);
 		const uint32_t cnt = __popc(N);
-		uint32_t incl = cnt;
-#pragma unroll
-		for (int d = 1; d < 32; d <<= 1) {
-			const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
-			if (lane >= d)
-				incl += o;
-		}
+		const uint32_t incl = row_scan(cnt);
 		const uint32_t start = incl - cnt;
 		const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
 		__syncwarp();
+		if (part == 0 && total <= 32) {
+			if (total == 0) { // only lone faces: nothing to key
+				if (any_face)
+					plane_count_one(S, p);
+				continue;
+			}
+			if (G.n == kGroupPlanes || G.total + total > 32)
+				key_group(S, G);
+			G.planes |= (uint32_t)p << (8 * G.n);
+			G.bases |= G.total << (8 * G.n);
+			G.total += total;
+			++G.n;
+			continue;
+		}
 		const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
 		Key prev{0, 0, 0};
 		uint32_t prev_b = 0, b = 0;
@@ -731,12 +874,8 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 			const uint32_t Nu = __shfl_sync(0xffffffffu, N, u);
 			const int v = has ? nth_set_bit(Nu, k) : 0;
 			Key key{0, 0, 0};
-			if (has) {
-				Light4 l;
-				key = face_key(S, a, s, inv, u, v, nullptr, &l);
-				if (S.keys) // kept for the emission of the quad this face may start
-					S.keys[p * 1024 + u * 32 + v] = pack_light4(l);
-			}
+			if (has)
+				key = face_key(S, a, s, inv, u, v, nullptr, nullptr);
 			// right neighbour: next lane when (u, v + 1) is visible
 			const Key right = shfl_down_key(key);
 			const bool rv = has && v < 31 && ((Nu >> (v + 1)) & 1u);
@@ -777,6 +916,7 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 			plane_count_one(S, p);
 		}
 	}
+	key_group(S, G);
 }
 
 // Exact greedy scan of one plane from its masks (BlockMeshAlgo.hpp:345-477), one warp per plane.
@@ -837,13 +977,11 @@ __device__ __forceinline__ void warp_merge_plane(const uint32_t (*m)[4], G &&on_
 	}
 }
 
-// Quad record: plane, row, column, width-1, height-1, stream, whether the first face's light key
-// is in the key scratch (it is not a lone face); then the quad's index among the plane's quads (all
-// streams) and among the plane's quads of its stream.
-__device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, int st, uint32_t li, uint32_t lk,
-                                             bool keyed = false) {
+// Quad record: plane, row, column, width-1, height-1, stream; then the quad's index among the
+// plane's quads (all streams) and among the plane's quads of its stream.
+__device__ __forceinline__ uint2 quad_record(int p, int u, int v, int w, int h, int st, uint32_t li, uint32_t lk) {
 	return make_uint2((uint32_t)p | ((uint32_t)u << 8) | ((uint32_t)v << 13) | ((uint32_t)(w - 1) << 18) |
-	                      ((uint32_t)(h - 1) << 23) | ((uint32_t)st << 28) | ((uint32_t)keyed << 29),
+	                      ((uint32_t)(h - 1) << 23) | ((uint32_t)st << 28),
 	                  li | (lk << 16));
 }
 
@@ -875,9 +1013,6 @@ __device__ void plane_count_one(Smem &S, int p) {
 	const uint32_t(*m)[4] = S.u.masks[p];
 	const uint32_t rN = m[lane][0], rE = m[lane][1], rD = m[lane][2], rT = m[lane][3];
 	const uint32_t rDup = __shfl_up_sync(0xffffffffu, rD, 1);
-	// lone faces (no visible face beside, above or below): the key pass left their keys out
-	const uint32_t rNu = __shfl_up_sync(0xffffffffu, rN, 1), rNd = __shfl_down_sync(0xffffffffu, rN, 1);
-	const uint32_t rLone = rN & ~(rN << 1) & ~(rN >> 1) & ~(lane == 0 ? 0u : rNu) & ~(lane == 31 ? 0u : rNd);
 	const bool iso = rD == 0 && (lane == 0 || rDup == 0);
 	const uint32_t icont = rN & (rN << 1) & (rE << 1); // bit v continues the run of v - 1
 	const uint32_t istarts = iso ? (rN & ~icont) : 0u;
@@ -902,15 +1037,13 @@ __device__ void plane_count_one(Smem &S, int p) {
 		const uint32_t cnt = __popc(starts), c1 = __popc(starts & tmask);
 		const uint32_t base = __shfl_sync(0xffffffffu, b, 0);
 		const uint32_t ex = __shfl_sync(0xffffffffu, iexcl, u); // isolated quads of the rows above u
-		const uint32_t lone_u = __shfl_sync(0xffffffffu, rLone, u);
 		if (is_start) {
 			const int st = (int)((tmask >> lane) & 1u);
 			const uint32_t same = st ? (starts & tmask) : (starts & ~tmask);
 			const uint32_t ex_all = ex & 0xffffu, ex_t = ex >> 16;
 			const uint32_t li = ex_all + b_all + __popc(starts & lt);
 			const uint32_t lk = (st ? ex_t + b_st[1] : ex_all - ex_t + b_st[0]) + __popc(same & lt);
-			const bool keyed = !((lone_u >> lane) & 1u);
-			put_record(S, base + __popc(starts & lt), quad_record(p, u, lane, w, h, st, li, lk, keyed));
+			put_record(S, base + __popc(starts & lt), quad_record(p, u, lane, w, h, st, li, lk));
 		}
 		if (lane == u)
 			mine = cnt | (c1 << 16);
@@ -930,7 +1063,7 @@ __device__ void plane_count_one(Smem &S, int p) {
 		const int w = __ffs(~after); // cells from v to the end of its run
 		const int st = (int)((rT >> v) & 1u);
 		const uint32_t lk = st ? e_t + k_t : e_all - e_t + (k_all - k_t);
-		put_record(S, j + k_all, quad_record(p, lane, v, w, 1, st, e_all + k_all, lk, !((rLone >> v) & 1u)));
+		put_record(S, j + k_all, quad_record(p, lane, v, w, 1, st, e_all + k_all, lk));
 		++k_all;
 		k_t += (uint32_t)st;
 	}
@@ -943,24 +1076,15 @@ __device__ void plane_count_one(Smem &S, int p) {
 
 // Writes quad (u, v, w, h) of plane p: stream st, stream index k, all-stream index g. Called by all
 // lanes of a warp; lanes without a quad (valid false) only take part in the box reduction.
-__device__ void emit_plane_quad(Smem &S, const Emit &E, bool valid, int p, int u, int v, int w, int h, int st, uint32_t k,
-                                uint32_t g, bool keyed = false) {
+__device__ void emit_plane_quad(Smem &S, const Emit &E, BoxAcc &box, bool valid, int p, int u, int v, int w, int h,
+                                int st, uint32_t k, uint32_t g) {
 	uint32_t mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
 	if (valid) {
 		const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
 		const bool uv_cycle = a != 2; // (U + 1) % 3 == V for the YZX swizzle (BlockMeshAlgo.hpp:384)
 		uint16_t t;
 		Light4 l;
-		if (keyed && S.keys) { // the key pass kept this face's light
-			int x, y, z;
-			to_xyz(a, s, u, v, x, y, z);
-			if (!inv)
-				(a == 0 ? x : (a == 1 ? y : z)) -= 1;
-			t = get_tex(S, x, y, z, 2 * a + inv);
-			l = unpack_light4(__ldcg(S.keys + p * 1024 + u * 32 + v));
-		} else {
-			face_key(S, a, s, inv, u, v, &t, &l);
-		}
+		face_key(S, a, s, inv, u, v, &t, &l);
 		int o[3], hv[3], wv[3];
 		to_xyz(a, s, u, v, o[0], o[1], o[2]);
 		to_xyz(a, 0, h, 0, hv[0], hv[1], hv[2]);
@@ -980,15 +1104,15 @@ __device__ void emit_plane_quad(Smem &S, const Emit &E, bool valid, int p, int u
 		mx[0] = (uint32_t)cx[2] << 4, mx[1] = (uint32_t)cy[2] << 4, mx[2] = (uint32_t)cz[2] << 4;
 		put_quad(S, E, st, k, g, vt, flip_of(l));
 	}
-	aabb_add_warp(S, valid, st, k / kQuadsPerMesh, mn, mx);
+	box_add_warp(S, box, valid, st, k / kQuadsPerMesh, mn, mx);
 }
 
-__device__ __forceinline__ void emit_record(Smem &S, const Emit &E, bool valid, uint2 r) {
+__device__ __forceinline__ void emit_record(Smem &S, const Emit &E, BoxAcc &box, bool valid, uint2 r) {
 	const int p = (int)(r.x & 255u), st = (int)((r.x >> 28) & 1u);
 	const uint32_t li = r.y & 0xffffu, lk = r.y >> 16;
-	emit_plane_quad(S, E, valid, p, (int)((r.x >> 8) & 31u), (int)((r.x >> 13) & 31u), (int)((r.x >> 18) & 31u) + 1,
+	emit_plane_quad(S, E, box, valid, p, (int)((r.x >> 8) & 31u), (int)((r.x >> 13) & 31u), (int)((r.x >> 18) & 31u) + 1,
 	                (int)((r.x >> 23) & 31u) + 1, st, valid ? S.seg_base[st][1 + p] + lk : 0u,
-	                valid ? S.seg_base[2][1 + p] + li : 0u, (r.x >> 29) & 1u);
+	                valid ? S.seg_base[2][1 + p] + li : 0u);
 }
 
 // Emits the plane quads this CTA owns. Normally plane_count_one kept all their records; otherwise
@@ -998,12 +1122,14 @@ __device__ __forceinline__ void emit_record(Smem &S, const Emit &E, bool valid, 
 // heavy plane does not wait on the warp that merges it.
 __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	BoxAcc box;
 	if (!S.misc[5]) {
 		const uint32_t n = S.misc[4];
 		for (uint32_t j0 = (uint32_t)warp * 32; j0 < n; j0 += kThreads) {
 			const uint32_t j = j0 + lane;
-			emit_record(S, E, j < n, j < n ? get_record(S, j) : make_uint2(0, 0));
+			emit_record(S, E, box, j < n, j < n ? get_record(S, j) : make_uint2(0, 0));
 		}
+		box_flush(S, box);
 		return;
 	}
 	// own-quad offset of each taken plane (one warp; up to kPlanes entries)
@@ -1058,10 +1184,11 @@ __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 		const uint32_t n = min((uint32_t)kQuadBuf, own_quads - w0);
 		for (uint32_t j0 = (uint32_t)warp * 32; j0 < n; j0 += kThreads) {
 			const uint32_t j = j0 + lane;
-			emit_record(S, E, j < n, j < n ? S.aux.quads[j] : make_uint2(0, 0));
+			emit_record(S, E, box, j < n, j < n ? S.aux.quads[j] : make_uint2(0, 0));
 		}
 		__syncthreads();
 	}
+	box_flush(S, box);
 }
 
 // --------------------------------------------------------------------------------------- scans
@@ -1147,7 +1274,7 @@ struct Arena {
 	unsigned long long quad_cap;
 	unsigned int mesh_cap;
 	uint32_t *results;     // per batch position: opaque quads, transparent quads, first mesh, mesh count, status
-	uint2 *spill = nullptr; // kCtaScratch words per CTA of the grid (blockIdx.x): records, then keys; or null
+	uint2 *spill = nullptr; // kSpillRecs quad records per CTA of the grid (blockIdx.x), or null
 };
 
 enum : uint32_t { kChunkOk = 0, kChunkCapacity = 1 };
@@ -1173,10 +1300,8 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 	             // cluster, the relight's) order this before any CTA's plane phases
 		S.misc[tid < 4 ? kClaimComplex + tid : tid] = 0;
 	if (tid == 0) {
-		uint2 *const mine = A.spill ? A.spill + (size_t)blockIdx.x * kCtaScratch : nullptr;
-		S.spill = mine;
-		S.spill_cap = mine ? kSpillRecs : 0u;
-		S.keys = mine ? mine + kSpillRecs : nullptr;
+		S.spill = A.spill ? A.spill + (size_t)blockIdx.x * kSpillRecs : nullptr;
+		S.spill_cap = A.spill ? kSpillRecs : 0u;
 	}
 	bool has_custom;
 	const bool blank = stage_classes(S, T, has_custom);

@@ -680,6 +680,89 @@ __device__ __forceinline__ uint64_t light_bytes8(const uint32_t w[8], int g) {
 	return x;
 }
 
+// The light-pass decode of one item of light_from_levels: item it < 34 * 34 is row (y, z) =
+// (it / 34 - 1, it % 34 - 1), x in [0, 32), returned as 32 light bytes in v[0..3] (true); the others
+// are the x = -1 and x = 32 edge pieces, written straight into the low bytes of their cells (false).
+__device__ __forceinline__ bool light_item(Smem &S, int it, uint64_t v[4]) {
+	constexpr int kRowItems = kLt * kLt;
+	uint8_t *light = light_bytes(S);
+	const uint32_t *src;
+	int stride, nb;
+	int x = 0, y, zc = 1, z0 = 0;
+	if (it < kRowItems) {
+		y = it / kLt - 1;
+		const int z = it % kLt - 1;
+		nb = nb_index(0, y, z);
+		src = S.lvl[nb] + (y & 31) * 32 + (z & 31);
+		stride = kPlaneWords;
+	} else {
+		const int k = it - kRowItems, side = k / (kLt * 3), rem = k - side * (kLt * 3);
+		y = rem / 3 - 1, zc = rem % 3;
+		x = side ? kChunk : -1, z0 = zc == 0 ? -1 : (zc == 1 ? 0 : kChunk);
+		nb = nb_index(x, y, z0);
+		src = S.edg[nb] + (side ? 0 : 32) + (y & 31); // x = 0 or x = 31 bits over z
+		stride = 64;
+	}
+	uint32_t b[2][4];
+#pragma unroll
+	for (int c = 0; c < 2; ++c) {
+		const uint32_t fl = S.lfl[nb][c]; // uniform planes are not stored
+		uint32_t lv[kLevels];
+#pragma unroll
+		for (int u = 0; u < kLevels; ++u)
+			lv[u] = level_word(fl, u + 1, src + (size_t)(c * kLevels + u) * stride);
+		level_bits(lv, b[c]);
+	}
+	const uint32_t w[8] = {b[0][0], b[0][1], b[0][2], b[0][3], b[1][0], b[1][1], b[1][2], b[1][3]};
+	if (it < kRowItems) {
+#pragma unroll
+		for (int g = 0; g < 4; ++g)
+			v[g] = light_bytes8(w, g);
+		return true;
+	}
+	if (zc == 1) { // 32 cells along z
+		uint8_t *dst = light + 2 * lt_index(x, y, 0);
+#pragma unroll
+		for (int g = 0; g < 4; ++g) {
+			const uint64_t q = light_bytes8(w, g);
+#pragma unroll
+			for (int j = 0; j < 8; ++j)
+				dst[2 * kLt * (8 * g + j)] = (uint8_t)(q >> (8 * j));
+		}
+	} else { // the corner cell z = -1 (bit 31 of the -z chunk) or z = 32 (bit 0 of the +z chunk)
+		const int bz = z0 & 31;
+		uint32_t q = 0;
+#pragma unroll
+		for (int bit = 0; bit < 8; ++bit)
+			q |= ((w[bit] >> bz) & 1u) << bit;
+		light[2 * lt_index(x, y, z0)] = (uint8_t)q;
+	}
+	return false;
+}
+
+// Writes the 32 cells x in [0, 32) of row item `row` (34 * (y + 1) + z + 1): light bytes from v,
+// class ids from the 32 bytes at `cls`. Cell 0 and cell 31 as halves, cells 1-30 as aligned pairs.
+__device__ __forceinline__ void write_row_cells(Smem &S, int row, const uint64_t v[4], const uint8_t *cls) {
+	uint16_t *c = S.cell + row * kCls + 1;
+	const uint4 k0 = *reinterpret_cast<const uint4 *>(cls), k1 = *reinterpret_cast<const uint4 *>(cls + 16);
+	const uint32_t kw[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+	const uint32_t lw[8] = {(uint32_t)v[0], (uint32_t)(v[0] >> 32), (uint32_t)v[1], (uint32_t)(v[1] >> 32),
+	                        (uint32_t)v[2], (uint32_t)(v[2] >> 32), (uint32_t)v[3], (uint32_t)(v[3] >> 32)};
+	// cell i = light byte i | class byte i << 8: the low and high byte pairs of each 4-cell group
+	uint32_t pair[16];
+#pragma unroll
+	for (int q = 0; q < 8; ++q) {
+		pair[2 * q] = __byte_perm(lw[q], kw[q], 0x5140);     // cells 4q, 4q + 1
+		pair[2 * q + 1] = __byte_perm(lw[q], kw[q], 0x7362); // cells 4q + 2, 4q + 3
+	}
+	c[0] = (uint16_t)pair[0];
+	uint32_t *c2 = reinterpret_cast<uint32_t *>(c + 1);
+#pragma unroll
+	for (int i = 0; i < 15; ++i) // cells 2i + 1, 2i + 2
+		c2[i] = __byte_perm(pair[i], pair[i + 1], 0x5432);
+	c[31] = (uint16_t)(pair[15] >> 16);
+}
+
 // Light of [-1, 32]^3 from the batch light pass (instead of relight_window), decoded from the 15
 // nested level planes per channel into the low byte of every staged cell: a cell's light is the
 // number of levels that hold it, read as four binary digits by level_bits. Cells x in [0, 32) of

@@ -699,7 +699,7 @@ hc_status hc_server_resident(hc_server *s, int32_t *cell_slots) {
 hc_pool *hc_server_pool(hc_server *s) { return s ? s->pool : nullptr; }
 
 hc_status hc_server_replay(hc_server *s, const hc_request *reqs, const uint64_t *arrival_ns, uint32_t n,
-                           uint64_t *latency_ns, uint64_t *elapsed_ns) {
+                           uint64_t *latency_ns, uint64_t *ticks, uint64_t *elapsed_ns) {
 	if (!s || (n && (!reqs || !arrival_ns || !latency_ns)) || !s->running.load())
 		return HC_ERR_INVALID_ARG;
 	{
@@ -742,6 +742,8 @@ hc_status hc_server_replay(hc_server *s, const hc_request *reqs, const uint64_t 
 			const hc_completion &c = buf[j];
 			if (c.tag < n) {
 				latency_ns[c.tag] = c.done_ns - c.submit_ns;
+				if (ticks)
+					ticks[c.tag] = c.tick;
 				last = std::max(last, c.done_ns);
 				++got;
 			}

@@ -94,7 +94,7 @@ def _bind(lib):
     lib.hc_server_resident.argtypes = [vp, vp]
     lib.hc_server_pool.argtypes = [vp]
     lib.hc_server_pool.restype = vp
-    lib.hc_server_replay.argtypes = [vp, vp, vp, u32, vp, P(u64)]
+    lib.hc_server_replay.argtypes = [vp, vp, vp, u32, vp, vp, P(u64)]
     lib._server_bound = True
     return lib
 
@@ -226,15 +226,18 @@ class Server:
         self._sink = SINK(cb)
         self.ctx.check(self.lib.hc_server_set_sink(self.handle, self._sink, None), "hc_server_set_sink")
 
-    def replay(self, reqs: np.ndarray, arrival_ns: np.ndarray):
-        """Real-time replay of a timed trace on a started server: (latency_ns per request, elapsed_ns)."""
+    def replay(self, reqs: np.ndarray, arrival_ns: np.ndarray, with_ticks: bool = False):
+        """Real-time replay of a timed trace on a started server: (latency_ns per request, elapsed_ns),
+        plus the tick that admitted each request when with_ticks."""
         r = np.ascontiguousarray(reqs, REQUEST_DTYPE)
         a = np.ascontiguousarray(arrival_ns, np.uint64)
         lat = np.zeros(len(r), np.uint64)
+        ticks = np.zeros(len(r), np.uint64) if with_ticks else None
         el = ctypes.c_uint64()
         self.ctx.check(self.lib.hc_server_replay(self.handle, r.ctypes.data, a.ctypes.data, len(r), lat.ctypes.data,
-                                                 ctypes.byref(el)), "hc_server_replay")
-        return lat, el.value
+                                                 ticks.ctypes.data if with_ticks else None, ctypes.byref(el)),
+                       "hc_server_replay")
+        return (lat, el.value, ticks) if with_ticks else (lat, el.value)
 
     def close(self):
         if getattr(self, "handle", None):

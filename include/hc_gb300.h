@@ -162,12 +162,19 @@ hc_status hc_mesh_infos(hc_ctx *ctx, const hc_mesh_desc *meshes, uint32_t n, con
 typedef struct hc_batch_plan hc_batch_plan;
 
 enum { HC_BATCH_PERSISTENT = 0, HC_BATCH_PER_CHUNK = 1, HC_BATCH_AUTO = 2 };
-/* Persistent-form variants (see HC_BATCH_AUTO): */
+/* Persistent-form variants (see HC_BATCH_AUTO): the relight (a batch light pass or a window per
+ * chunk), CTAs per chunk, chunks a CTA takes per claim of the work counter, and the emission
+ * scheme (quad records past shared memory kept in a global scratch, or no scratch: the emission
+ * merges the planes again in windows of records). */
 enum {
-	HC_VARIANT_LIGHT_PASS = 0, /* batch light pass, then one CTA per chunk */
+	HC_VARIANT_LIGHT_PASS = 0, /* batch light pass, one CTA per chunk, 1 chunk per claim, record scratch */
 	HC_VARIANT_WINDOW = 1,     /* each chunk relights its own 62^3 window, one CTA per chunk */
 	HC_VARIANT_CLUSTER2 = 2,   /* window relight, two CTAs (a cluster) per chunk */
-	HC_VARIANT_CLUSTER4 = 3    /* window relight, four CTAs per chunk */
+	HC_VARIANT_CLUSTER4 = 3,   /* window relight, four CTAs per chunk */
+	HC_VARIANT_CLAIM2 = 4,     /* as HC_VARIANT_LIGHT_PASS, 2 chunks per claim */
+	HC_VARIANT_CLAIM4 = 5,     /* as HC_VARIANT_LIGHT_PASS, 4 chunks per claim */
+	HC_VARIANT_NO_SCRATCH = 6, /* as HC_VARIANT_LIGHT_PASS, quad records in shared memory only */
+	HC_VARIANT_COUNT = 7
 };
 /* Mode that builds exactly one persistent variant (no timing), e.g. to profile the one an
  * HC_BATCH_AUTO plan chose: a profiler's per-launch cost distorts the autotuner's own timing. */
@@ -184,8 +191,8 @@ hc_status hc_batch_plan_create(hc_ctx *ctx, hc_pool *pool, const int32_t *neighb
                                const hc_batch_arena *arena, int mode, int ctas_per_sm, hc_batch_plan **out);
 void hc_batch_plan_destroy(hc_batch_plan *plan);
 /* The persistent variant the plan runs and, after HC_BATCH_AUTO, the time each variant took on
- * the batch (ms; 0 where not timed). */
-hc_status hc_batch_plan_variant(const hc_batch_plan *plan, int *variant, float ms[4]);
+ * the batch (ms per variant, HC_VARIANT_COUNT entries; 0 where not timed). */
+hc_status hc_batch_plan_variant(const hc_batch_plan *plan, int *variant, float ms[HC_VARIANT_COUNT]);
 /* Waits for the last launch and gives the device time of its stages (ms, CUDA events recorded
  * inside the plan): [0] bit-plane refresh, [1] batch light pass (0 for other variants), [2] the
  * meshing kernel(s). No counterpart in the reference (its runner is not staged). */
@@ -374,9 +381,10 @@ hc_status hc_server_resident(hc_server *server, int32_t *cell_slots);
 hc_pool *hc_server_pool(hc_server *server);
 /* Replays a timed request trace on a started server: request i is submitted arrival_ns[i] after
  * the call starts (its tag becomes i); returns once all have completed, with latency_ns[i] from
- * its arrival time to its completion and *elapsed_ns from the start to the last completion. */
+ * its arrival time to its completion, ticks[i] the tick that admitted it (ticks may be NULL) and
+ * *elapsed_ns from the start to the last completion. */
 hc_status hc_server_replay(hc_server *server, const hc_request *requests, const uint64_t *arrival_ns, uint32_t n,
-                           uint64_t *latency_ns, uint64_t *elapsed_ns);
+                           uint64_t *latency_ns, uint64_t *ticks, uint64_t *elapsed_ns);
 
 /* ----------------------------------------------------------------------------------------------
  * Batched meshing that allocates nothing. No counterpart in the reference.

@@ -12,10 +12,11 @@ def _small_world(kind):
 
 
 @pytest.mark.parametrize("kind", ["scale", "mixture"])
-@pytest.mark.parametrize("mode", [0, 1, 2, 17, 18, 19])
+@pytest.mark.parametrize("mode", [0, 1, 2, 17, 18, 19, 20, 21, 22])
 def test_batch_matches_oracle(ctx, oracle, kind, mode):
     """Persistent plan, per-chunk plan, the autotuned plan (whichever variant it keeps) and each
-    other persistent variant pinned (window relight on one, two and four CTAs per chunk)."""
+    other persistent variant pinned (window relight on one, two and four CTAs per chunk; 2 and 4
+    chunks per claim; no global record scratch)."""
     from hypercraft_gb300 import batch
     w = _small_world(kind)
     rw = batch.upload_world(ctx, w)
@@ -40,7 +41,7 @@ def test_batch_matches_oracle(ctx, oracle, kind, mode):
     assert total == q
 
 
-@pytest.mark.parametrize("mode", [0, 17, 18, 19])
+@pytest.mark.parametrize("mode", [0, 17, 18, 19, 20, 21, 22])
 def test_batch_most_quads_match_oracle(ctx, oracle, mode):
     """The 196,608-quad chunk through each persistent variant (records past the shared buffer and
     the global scratch: the emission merges again in windows)."""

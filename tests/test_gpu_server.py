@@ -1,6 +1,7 @@
 """Request server on the device: a seeded serving trace (edits, 16^3 fills, loads and unloads
 along a player walk) replayed in real time, many requests per tick, against the same trace run one
-request per tick; and the meshes the one-at-a-time run produces against the oracle."""
+request per tick and against each tick's requests run alone; and the meshes the one-at-a-time run
+produces against the oracle."""
 import numpy as np
 import pytest
 
@@ -120,6 +121,56 @@ def test_same_result_alone_and_in_the_mix(ctx, oracle, library):
     assert len(steady) >= 10
     for c in steady:
         assert _meshes_equal(latest_alone[c], latest_mix.get(c)), c
+    alone.close()
+    mix.close()
+
+
+def test_every_pass_same_alone_and_in_the_mix(ctx, library):
+    """Every pass of the real-time mix, run again alone: the requests that one tick of the mix
+    admitted are submitted together to a fresh server and run as one pass, with nothing else in
+    flight. Each pass remeshes the same chunks, in the same order, with the same meshes."""
+    init, reqs, times = _trace(library, seed=5)
+    mix = _server(ctx)
+    passes_mix = {}
+
+    def sink_mix(tick, cells, meshes, status):
+        passes_mix[int(tick)] = ([int(c) for c in cells], list(meshes), [int(x) for x in status])
+
+    mix.set_sink(sink_mix)
+    mix.submit(init)
+    mix.drain()
+    passes_mix.clear()
+    mix.start()
+    _, _, ticks = mix.replay(reqs, times, with_ticks=True)
+    mix.stop()
+    groups = sorted(set(int(t) for t in ticks))
+    assert len(groups) < len(reqs), "requests were batched"
+    assert set(t for t, p in passes_mix.items() if p[0]) <= set(groups), "a pass without admitted requests"
+
+    alone = _server(ctx)
+    last = {}
+
+    def sink_alone(tick, cells, meshes, status):
+        last["pass"] = ([int(c) for c in cells], list(meshes), [int(x) for x in status])
+
+    alone.set_sink(sink_alone)
+    alone.submit(init)
+    alone.drain()
+    remeshed = 0
+    for t in groups:
+        group = reqs[ticks == t]
+        last.clear()
+        alone.submit(group)
+        assert alone.step() == len(group), t
+        got = last.get("pass", ([], [], []))
+        want = passes_mix.get(t, ([], [], []))
+        assert got[0] == want[0], t
+        assert got[2] == want[2], t
+        for i, c in enumerate(got[0]):
+            if got[2][i] == 0:
+                assert _meshes_equal(got[1][i], want[1][i]), (t, c)
+        remeshed += len(got[0])
+    assert remeshed >= 20
     alone.close()
     mix.close()
 
