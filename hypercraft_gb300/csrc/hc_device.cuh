@@ -15,7 +15,8 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 32;
 constexpr int kQuadsPerMesh = 16383;       // 65,532 vertices: the uint16 split point (BlockMeshAlgo.hpp:274)
 constexpr int kMaxMeshesPerStream = 48;    // > 720,896 / 16,383
-constexpr int kMaxSplit = 4;               // face planes keyed in two halves per chunk, at most
+constexpr int kMaxSplit = 4;               // face planes keyed in row parts per chunk, at most
+constexpr int kMaxParts = 4;               // row parts of a split face plane, at most
 constexpr int kPlanes = 198;               // 3 axes x 33 slices x 2 face directions
 constexpr int kSlices = 99;
 constexpr int kSegments = kPlanes + 1;     // segment 0 = custom meshes, then the planes in output order
@@ -159,9 +160,10 @@ struct Smem {
 	uint8_t row_of[kWarps][32];   // per warp, key pass: the row whose faces start at each lane of a batch
 	// face planes keyed in two halves (the heaviest): the visible and complex words of the row above
 	// the second half, the second half's first row, and how many halves are done
-	uint32_t split_side[kMaxSplit][2];
+	uint32_t split_side[kMaxSplit][kMaxParts][2]; // part q >= 1: visible and complex words of its first row - 1
 	uint32_t split_done[kMaxSplit];
-	uint8_t split_row[kMaxSplit];
+	uint8_t split_rows[kMaxSplit][kMaxParts + 1]; // part q keys rows [rows[q], rows[q + 1])
+	uint8_t split_first[kMaxSplit + 1];           // claim index of each split plane's first part
 };
 
 static_assert(offsetof(Smem, u) % 16 == 0, "plane mask rows are written as 16-byte words");

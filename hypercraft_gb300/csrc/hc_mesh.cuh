@@ -661,11 +661,12 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t x, uint32_t *total) 
 	return incl - x;
 }
 
-// Heavy face planes (weight >= kSplitMin, the kMaxSplit heaviest) are keyed in two row halves by
-// two warps, so that the heaviest plane does not hold the key phase open; the warp that finishes
-// second merges and counts the plane. The split row balances the weights (visible faces and complex
-// candidates) of the halves. The row above the second half is keyed by both: the second half reads
-// its visible and complex words from a copy taken here, as the first half rewrites them.
+// Heavy face planes (weight >= kSplitMin, the kMaxSplit heaviest) are keyed in row parts by
+// several warps (two, three or four parts by weight), so that the heaviest plane does not hold the
+// key phase open; the warp that finishes last merges and counts the plane. The split rows balance
+// the weights (visible faces and complex candidates) of the parts. The row above each part after the
+// first is keyed by that part too (for the equal-below bits of that row): it reads the row's visible
+// and complex words from a copy taken here, as the part before rewrites them.
 constexpr uint32_t kSplitMin = 128;
 
 // After order_planes (plane weights in seg_base). Returns how many planes are split (every thread).
@@ -677,32 +678,54 @@ __device__ int split_heavy_planes(Smem &S, int live) {
 		const uint32_t w = __popc(S.u.masks[p][lane][0] | S.u.masks[p][lane][1]);
 		uint32_t tot;
 		const uint32_t ex = warp_excl_scan(w, &tot);
-		const int r = max(__ffs(__ballot_sync(0xffffffffu, 2 * (ex + w) > tot)) - 1, 1);
+		const int parts = tot >= 3 * kSplitMin ? 4 : (tot >= 2 * kSplitMin ? 3 : 2);
+		int prev = 0;
+		for (int q = 1; q < parts; ++q) { // part q starts at the row where the weight passes q / parts
+			int r = __ffs(__ballot_sync(0xffffffffu, (ex + w) * (uint32_t)parts > (uint32_t)q * tot)) - 1;
+			r = min(max(r, prev + 1), 32 - (parts - q));
+			if (lane == 0) {
+				S.split_rows[warp][q] = (uint8_t)r;
+				S.split_side[warp][q][0] = S.u.masks[p][r - 1][0];
+				S.split_side[warp][q][1] = S.u.masks[p][r - 1][1];
+			}
+			prev = r;
+		}
 		if (lane == 0) {
-			S.split_row[warp] = (uint8_t)r;
-			S.split_side[warp][0] = S.u.masks[p][r - 1][0];
-			S.split_side[warp][1] = S.u.masks[p][r - 1][1];
+			S.split_rows[warp][0] = 0;
+			S.split_rows[warp][parts] = 32;
+			S.split_first[warp + 1] = (uint8_t)parts; // a count here; turned into offsets below
 			S.split_done[warp] = 0;
 		}
 	}
-	return __syncthreads_count((int)threadIdx.x < kMaxSplit && (int)threadIdx.x < live &&
-	                           weight[S.order[threadIdx.x]] >= kSplitMin);
+	const int nsplit = __syncthreads_count((int)threadIdx.x < kMaxSplit && (int)threadIdx.x < live &&
+	                                       weight[S.order[threadIdx.x]] >= kSplitMin);
+	if (threadIdx.x == 0) { // the heaviest planes are split, so the split ones are order[0, nsplit)
+		S.split_first[0] = 0;
+		for (int k = 0; k < nsplit; ++k)
+			S.split_first[k + 1] = (uint8_t)(S.split_first[k] + S.split_first[k + 1]);
+	}
+	__syncthreads();
+	return nsplit;
 }
 
-// Next key-pass item for the calling warp: plane | part << 8 | split index << 10, part 0 = the whole
-// plane, 1 / 2 = the first / second half of split plane k. The halves of the split planes come
-// first, then the other planes heaviest first. A whole plane is recorded as this CTA's when taken,
-// a split one by the warp that merges it.
+// Next key-pass item for the calling warp: plane | part << 8 | split index << 12, part 0 = the whole
+// plane, q + 1 = part q of split plane k. The parts of the split planes come first, then the other
+// planes heaviest first. A whole plane is recorded as this CTA's when taken, a split one by the
+// warp that merges it.
 __device__ __forceinline__ int claim_item(Smem &S, const Split &sp, int live, int nsplit) {
 	if (sp.c > 1)
 		return claim_plane(S, sp, live);
 	int r = kPlanes;
 	if ((threadIdx.x & 31) == 0) {
 		const int j = (int)atomicAdd(&S.misc[kClaimKeys], 1u);
-		if (j < 2 * nsplit) {
-			r = (int)S.order[j >> 1] | ((1 + (j & 1)) << 8) | ((j >> 1) << 10);
+		const int nparts = S.split_first[nsplit];
+		if (j < nparts) {
+			int k = 0;
+			while (j >= S.split_first[k + 1])
+				++k;
+			r = (int)S.order[k] | ((1 + j - S.split_first[k]) << 8) | (k << 12);
 		} else {
-			const int jj = j - nsplit;
+			const int jj = j - nparts + nsplit;
 			r = jj < live ? (int)S.order[jj] : kPlanes;
 			if (r < kPlanes)
 				S.mine[atomicAdd(&S.misc[kMine], 1u)] = (uint8_t)r;
@@ -816,10 +839,10 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	PlaneGroup G;
 	for (int item = claim_item(S, sp, live, nsplit); (item & 255) < kPlanes; item = claim_item(S, sp, live, nsplit)) {
-		const int p = item & 255, part = (item >> 8) & 3, ks = item >> 10;
-		const int r0 = part == 2 ? (int)S.split_row[ks] : 0, r1 = part == 1 ? (int)S.split_row[ks] : 32;
+		const int p = item & 255, part = (item >> 8) & 15, ks = item >> 12;
+		const int r0 = part ? (int)S.split_rows[ks][part - 1] : 0, r1 = part ? (int)S.split_rows[ks][part] : 32;
 		const int lo = r0 > 0 ? r0 - 1 : 0;
-		const uint32_t V = plane_complex_one(S, p, lo, r0, r1, part == 2 ? S.split_side[ks] : nullptr);
+		const uint32_t V = plane_complex_one(S, p, lo, r0, r1, part > 1 ? S.split_side[ks][part - 1] : nullptr);
 		uint32_t *mrow = S.u.masks[p][lane];
 		if (lane >= r0 && lane < r1)
 			mrow[1] = 0;
@@ -904,12 +927,12 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 				plane_count_one(S, p);
 			continue;
 		}
-		// a half: the warp that finishes second merges the plane (its masks are complete then)
+		// a part: the warp that finishes last merges the plane (its masks are complete then)
 		__threadfence_block();
-		uint32_t first_done = 0;
+		uint32_t done_before = 0;
 		if (lane == 0)
-			first_done = atomicAdd(&S.split_done[ks], 1u);
-		if (__shfl_sync(0xffffffffu, first_done, 0) == 1u) {
+			done_before = atomicAdd(&S.split_done[ks], 1u);
+		if (__shfl_sync(0xffffffffu, done_before, 0) + 1u == (uint32_t)(S.split_first[ks + 1] - S.split_first[ks])) {
 			__threadfence_block();
 			if (lane == 0)
 				S.mine[atomicAdd(&S.misc[kMine], 1u)] = (uint8_t)p;
@@ -1052,20 +1075,25 @@ __device__ void plane_count_one(Smem &S, int p) {
 		b_st[0] += cnt - c1;
 	}, scanned);
 
-	// the isolated rows' quads, lane = row
+	// the isolated rows' quads: row by row, lane = column, so that a row's records are written by
+	// one coalesced store (lane = row would scatter each store over 32 rows' records)
 	uint32_t btot;
 	const uint32_t e = iexcl + (scanned ? warp_excl_scan(mine, &btot) : 0u);
-	const uint32_t e_all = e & 0xffffu, e_t = e >> 16;
-	uint32_t j = ibase + (iexcl & 0xffffu), k_all = 0, k_t = 0;
-	for (uint32_t rest = istarts; rest; rest &= rest - 1u) {
-		const int v = __ffs(rest) - 1;
-		const uint32_t after = v == 31 ? 0u : (icont >> (v + 1));
-		const int w = __ffs(~after); // cells from v to the end of its run
-		const int st = (int)((rT >> v) & 1u);
-		const uint32_t lk = st ? e_t + k_t : e_all - e_t + (k_all - k_t);
-		put_record(S, j + k_all, quad_record(p, lane, v, w, 1, st, e_all + k_all, lk));
-		++k_all;
-		k_t += (uint32_t)st;
+	const uint32_t j = ibase + (iexcl & 0xffffu); // the row's first record slot
+	for (uint32_t rows_left = __ballot_sync(0xffffffffu, istarts != 0); rows_left; rows_left &= rows_left - 1u) {
+		const int u = __ffs(rows_left) - 1;
+		const uint32_t su = __shfl_sync(0xffffffffu, istarts, u), cu = __shfl_sync(0xffffffffu, icont, u);
+		const uint32_t tu = __shfl_sync(0xffffffffu, rT, u), eu = __shfl_sync(0xffffffffu, e, u);
+		const uint32_t ju = __shfl_sync(0xffffffffu, j, u);
+		if ((su >> lane) & 1u) {
+			const uint32_t e_all = eu & 0xffffu, e_t = eu >> 16;
+			const uint32_t k_all = __popc(su & lt), k_t = __popc(su & tu & lt); // quads of the row before it
+			const uint32_t after = lane == 31 ? 0u : (cu >> (lane + 1));
+			const int w = __ffs(~after); // cells from this column to the end of its run
+			const int st = (int)((tu >> lane) & 1u);
+			const uint32_t lk = st ? e_t + k_t : e_all - e_t + (k_all - k_t);
+			put_record(S, ju + k_all, quad_record(p, u, lane, w, 1, st, e_all + k_all, lk));
+		}
 	}
 	if (lane == 0) {
 		const uint32_t t1 = (itot >> 16) + b_st[1];
