@@ -1075,24 +1075,41 @@ __device__ void plane_count_one(Smem &S, int p) {
 		b_st[0] += cnt - c1;
 	}, scanned);
 
-	// the isolated rows' quads: row by row, lane = column, so that a row's records are written by
-	// one coalesced store (lane = row would scatter each store over 32 rows' records)
+	// the isolated rows' quads. Rows with many quads (a checkerboard's 16) are taken row by row,
+	// lane = column, so that a row's records are written by one coalesced store; otherwise lane =
+	// row, each lane walking its row's few quads.
 	uint32_t btot;
 	const uint32_t e = iexcl + (scanned ? warp_excl_scan(mine, &btot) : 0u);
 	const uint32_t j = ibase + (iexcl & 0xffffu); // the row's first record slot
-	for (uint32_t rows_left = __ballot_sync(0xffffffffu, istarts != 0); rows_left; rows_left &= rows_left - 1u) {
-		const int u = __ffs(rows_left) - 1;
-		const uint32_t su = __shfl_sync(0xffffffffu, istarts, u), cu = __shfl_sync(0xffffffffu, icont, u);
-		const uint32_t tu = __shfl_sync(0xffffffffu, rT, u), eu = __shfl_sync(0xffffffffu, e, u);
-		const uint32_t ju = __shfl_sync(0xffffffffu, j, u);
-		if ((su >> lane) & 1u) {
-			const uint32_t e_all = eu & 0xffffu, e_t = eu >> 16;
-			const uint32_t k_all = __popc(su & lt), k_t = __popc(su & tu & lt); // quads of the row before it
-			const uint32_t after = lane == 31 ? 0u : (cu >> (lane + 1));
-			const int w = __ffs(~after); // cells from this column to the end of its run
-			const int st = (int)((tu >> lane) & 1u);
+	const uint32_t irows = __ballot_sync(0xffffffffu, istarts != 0);
+	if ((itot & 0xffffu) >= 12u * (uint32_t)__popc(irows)) {
+		for (uint32_t rows_left = irows; rows_left; rows_left &= rows_left - 1u) {
+			const int u = __ffs(rows_left) - 1;
+			const uint32_t su = __shfl_sync(0xffffffffu, istarts, u), cu = __shfl_sync(0xffffffffu, icont, u);
+			const uint32_t tu = __shfl_sync(0xffffffffu, rT, u), eu = __shfl_sync(0xffffffffu, e, u);
+			const uint32_t ju = __shfl_sync(0xffffffffu, j, u);
+			if ((su >> lane) & 1u) {
+				const uint32_t e_all = eu & 0xffffu, e_t = eu >> 16;
+				const uint32_t k_all = __popc(su & lt), k_t = __popc(su & tu & lt); // the row's quads before it
+				const uint32_t after = lane == 31 ? 0u : (cu >> (lane + 1));
+				const int w = __ffs(~after); // cells from this column to the end of its run
+				const int st = (int)((tu >> lane) & 1u);
+				const uint32_t lk = st ? e_t + k_t : e_all - e_t + (k_all - k_t);
+				put_record(S, ju + k_all, quad_record(p, u, lane, w, 1, st, e_all + k_all, lk));
+			}
+		}
+	} else {
+		const uint32_t e_all = e & 0xffffu, e_t = e >> 16;
+		uint32_t k_all = 0, k_t = 0;
+		for (uint32_t rest = istarts; rest; rest &= rest - 1u) {
+			const int v = __ffs(rest) - 1;
+			const uint32_t after = v == 31 ? 0u : (icont >> (v + 1));
+			const int w = __ffs(~after); // cells from v to the end of its run
+			const int st = (int)((rT >> v) & 1u);
 			const uint32_t lk = st ? e_t + k_t : e_all - e_t + (k_all - k_t);
-			put_record(S, ju + k_all, quad_record(p, u, lane, w, 1, st, e_all + k_all, lk));
+			put_record(S, j + k_all, quad_record(p, lane, v, w, 1, st, e_all + k_all, lk));
+			++k_all;
+			k_t += (uint32_t)st;
 		}
 	}
 	if (lane == 0) {
