@@ -36,36 +36,64 @@ __device__ __forceinline__ int claim(uint32_t *counter) {
 }
 enum : int { kClaimComplex = 12, kClaimKeys = 13, kMine = 15 }; // S.misc counters
 
-// Orders the face planes by falling weight (visible faces and complex candidates, a tie to the
-// lower plane) into S.order, so that the key pass takes the heaviest planes first and its last
-// planes are light ones (longest-first scheduling). Weights sit in seg_base, unused until the scan.
-// Every CTA of a cluster computes the same order from the same masks. Returns how many planes have
-// any face: the rest are left out of the key pass (their counts stay 0; their owner is CTA 0).
+// Orders the face planes by falling weight class (visible faces and complex candidates; class =
+// the weight's bit length, so the weights of a class are within a factor of two) into S.order, so
+// that the key pass takes the heaviest planes first and its last planes are light ones
+// (longest-processing-time order, to a factor of two), planes of a class in plane order. A counting
+// sort: every thread of the first warps takes one plane and finds its rank from per-warp class
+// counts (warp match), so the order is the same on every run and in every CTA of a cluster (they
+// compute it from the same masks). Weights sit in seg_base[0], the count tables in seg_base[1],
+// both unused until the scan. Returns how many planes have any face: the rest are left out of the
+// key pass (their counts stay 0; their owner is CTA 0).
 __device__ int order_planes(Smem &S) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	constexpr int kClasses = 12, kOrderWarps = (kPlanes + 31) / 32; // weight <= 1,024: bit length <= 11
+	static_assert(2 * kClasses * kOrderWarps <= kSegments + 1, "count tables fit in seg_base[1]");
 	uint32_t *weight = &S.seg_base[0][0];
+	uint32_t *cnt = &S.seg_base[1][0], *base = cnt + kClasses * kOrderWarps; // [warp][class]
 	for (int p = warp; p < kPlanes; p += kWarps) {
 		const uint32_t w = __reduce_add_sync(0xffffffffu, __popc(S.u.masks[p][lane][0] | S.u.masks[p][lane][1]));
 		if (lane == 0)
 			weight[p] = w;
 	}
+	if (threadIdx.x < kClasses * kOrderWarps)
+		cnt[threadIdx.x] = 0;
 	__syncthreads();
-	{ // rank of plane p = planes before it; four neighbouring threads count a quarter each
-		const int p = threadIdx.x >> 2, part = threadIdx.x & 3;
+	const int p = threadIdx.x;
+	uint32_t cls = 0, before = 0; // this plane's class, and planes of its class earlier in its warp
+	if (warp < kOrderWarps) {
 		const uint32_t w = p < kPlanes ? weight[p] : 0u;
-		int rank = 0;
-		if (p < kPlanes)
-			for (int q = part; q < kPlanes; q += 4) {
-				const uint32_t wq = weight[q];
-				rank += (wq > w) || (wq == w && q < p);
-			}
-		rank += __shfl_xor_sync(0xffffffffu, rank, 1);
-		rank += __shfl_xor_sync(0xffffffffu, rank, 2);
-		if (p < kPlanes && part == 0) {
-			S.order[rank] = (uint8_t)p;
-			if (w == 0)
-				S.plane_owner[p] = 0;
+		cls = w ? 32u - __clz(w) : 0u;
+		const uint32_t peers = __match_any_sync(0xffffffffu, p < kPlanes ? cls : 0xffu);
+		before = __popc(peers & ((1u << lane) - 1u));
+		if (p < kPlanes && before == 0)
+			cnt[warp * kClasses + cls] = __popc(peers);
+	}
+	__syncthreads();
+	if (warp == 0) { // lane = class: planes in heavier classes, then in earlier warps of the same class
+		uint32_t tot = 0;
+		if (lane < kClasses)
+			for (int k = 0; k < kOrderWarps; ++k)
+				tot += cnt[k * kClasses + lane];
+		uint32_t heavier = tot; // becomes the sum over classes >= lane, then > lane
+#pragma unroll
+		for (int d = 1; d < 16; d <<= 1) {
+			const uint32_t o = __shfl_down_sync(0xffffffffu, heavier, d);
+			if (lane + d < kClasses)
+				heavier += o;
 		}
+		uint32_t run = heavier - tot;
+		if (lane < kClasses)
+			for (int k = 0; k < kOrderWarps; ++k) {
+				base[k * kClasses + lane] = run;
+				run += cnt[k * kClasses + lane];
+			}
+	}
+	__syncthreads();
+	if (warp < kOrderWarps && p < kPlanes) {
+		S.order[base[warp * kClasses + cls] + before] = (uint8_t)p;
+		if (weight[p] == 0)
+			S.plane_owner[p] = 0;
 	}
 	return __syncthreads_count(threadIdx.x < kPlanes && weight[threadIdx.x] > 0);
 }
