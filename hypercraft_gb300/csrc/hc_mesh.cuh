@@ -701,7 +701,18 @@ constexpr uint32_t kSplitMin = 128;
 __device__ int split_heavy_planes(Smem &S, int live) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t *weight = &S.seg_base[0][0];
-	if (warp < kMaxSplit && warp < live && weight[S.order[warp]] >= kSplitMin) {
+	// the split planes are the longest prefix of the order (at most kMaxSplit) whose weights reach
+	// kSplitMin, so that split plane k is order[k]
+	__shared__ int s_nsplit;
+	if (threadIdx.x == 0) {
+		int k = 0;
+		while (k < kMaxSplit && k < live && weight[S.order[k]] >= kSplitMin)
+			++k;
+		s_nsplit = k;
+	}
+	__syncthreads();
+	const int nsplit = s_nsplit;
+	if (warp < nsplit) {
 		const int p = S.order[warp];
 		const uint32_t w = __popc(S.u.masks[p][lane][0] | S.u.masks[p][lane][1]);
 		uint32_t tot;
@@ -725,9 +736,8 @@ __device__ int split_heavy_planes(Smem &S, int live) {
 			S.split_done[warp] = 0;
 		}
 	}
-	const int nsplit = __syncthreads_count((int)threadIdx.x < kMaxSplit && (int)threadIdx.x < live &&
-	                                       weight[S.order[threadIdx.x]] >= kSplitMin);
-	if (threadIdx.x == 0) { // the heaviest planes are split, so the split ones are order[0, nsplit)
+	__syncthreads();
+	if (threadIdx.x == 0) {
 		S.split_first[0] = 0;
 		for (int k = 0; k < nsplit; ++k)
 			S.split_first[k + 1] = (uint8_t)(S.split_first[k] + S.split_first[k + 1]);
@@ -791,81 +801,14 @@ __device__ __forceinline__ uint32_t row_scan(uint32_t cnt) {
 	return incl;
 }
 
-// Small whole planes (at most 32 keyed faces each) are keyed together: a group of up to four such
-// planes fills one warp's lanes, so that the light of a sparse plane's faces is not computed by a
-// warp that is mostly idle. kGroupPlanes planes at most; the group is packed in two words per warp.
-constexpr int kGroupPlanes = 4;
-struct PlaneGroup {
-	uint32_t planes = 0; // plane ids, 8 bits each
-	uint32_t bases = 0;  // first lane of each plane, 8 bits each
-	int n = 0;           // planes in the group
-	uint32_t total = 0;  // lanes used
-};
-
-// Keys the faces of every plane of the group in one batch (each plane's faces fit in it whole, so
-// a face's right and upper neighbours are in the same batch), sets their equal-right and
-// equal-below bits, then merges and counts each plane. Empties the group.
-__device__ void key_group(Smem &S, PlaneGroup &G) {
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	if (G.n == 0)
-		return;
-	int my_p = 0, my_u = 0, my_v = 0, my_up = -1; // this lane's face, and the lane of its upper neighbour
-	uint32_t my_Nu = 0;
-	for (int g = 0; g < G.n; ++g) { // warp-uniform
-		const int p = (int)((G.planes >> (8 * g)) & 255u);
-		const uint32_t base = (G.bases >> (8 * g)) & 255u;
-		const uint32_t end = g + 1 < G.n ? (G.bases >> (8 * (g + 1))) & 255u : G.total;
-		const uint32_t N = keyed_faces(S.u.masks[p][lane][0], 0, 32);
-		const uint32_t cnt = __popc(N), incl = row_scan(cnt), start = incl - cnt;
-		// rows holding faces record themselves where their faces start (distinct lanes)
-		const uint32_t M = __reduce_or_sync(0xffffffffu, cnt ? 1u << start : 0u);
-		if (cnt)
-			S.row_of[warp][start] = (uint8_t)lane;
-		__syncwarp();
-		const bool mine = lane >= (int)base && lane < (int)end;
-		const uint32_t f = mine ? lane - base : 0u; // face index in the plane
-		const int u = mine ? S.row_of[warp][31 - __clz(M & (f == 31 ? 0xffffffffu : ((2u << f) - 1u)))] : 0;
-		__syncwarp();
-		const uint32_t su = __shfl_sync(0xffffffffu, start, u), Nu = __shfl_sync(0xffffffffu, N, u);
-		const uint32_t Nup = __shfl_sync(0xffffffffu, N, (u + 31) & 31), sup = __shfl_sync(0xffffffffu, start, (u + 31) & 31);
-		if (mine) {
-			const int v = nth_set_bit(Nu, f - su);
-			my_p = p, my_u = u, my_v = v, my_Nu = Nu;
-			my_up = u > 0 && ((Nup >> v) & 1u) ? (int)(base + sup + __popc(Nup & ((1u << v) - 1u))) : -1;
-		}
-	}
-	const bool has = lane < (int)G.total;
-	Key key{0, 0, 0};
-	if (has) {
-		const int a = my_p / 66, s = (my_p % 66) >> 1, inv = my_p & 1;
-		key = face_key(S, a, s, inv, my_u, my_v, nullptr, nullptr);
-	}
-	// right neighbour: the next lane when (u, v + 1) is visible (then it is keyed, in the same plane)
-	const Key right = shfl_down_key(key);
-	if (has && my_v < 31 && ((my_Nu >> (my_v + 1)) & 1u) && key_eq(key, right))
-		atomicOr(&S.u.masks[my_p][my_u][1], 1u << my_v);
-	// upper neighbour (u - 1, v)
-	const int src = my_up < 0 ? lane : my_up;
-	const Key up{__shfl_sync(0xffffffffu, key.tex_ao, src), __shfl_sync(0xffffffffu, key.sun, src),
-	             __shfl_sync(0xffffffffu, key.torch, src)};
-	if (has && my_up >= 0 && key_eq(key, up))
-		atomicOr(&S.u.masks[my_p][my_u - 1][2], 1u << my_v);
-	__syncwarp();
-	for (int g = 0; g < G.n; ++g)
-		plane_count_one(S, (int)((G.planes >> (8 * g)) & 255u));
-	G = PlaneGroup{};
-}
-
 // Pass 2 (after the relight): equal-to-right and equal-to-below masks of every plane, each plane
 // then merged and counted by the warp that built its masks (no block barrier in between). The visible
 // faces of a plane are taken in batches of whole rows (at most 32 faces), one face per lane, so
 // the light keys are computed by full warps; a face's right neighbour is the next lane and its
 // upper neighbour sits in this batch or in the previous one. A half plane keys rows [lo, r1) and
 // writes the equal-right bits of rows [r0, r1) and the equal-below bits of rows [lo, r1 - 1).
-// Whole planes with at most 32 keyed faces go into the warp's plane group instead (key_group).
 __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	PlaneGroup G;
 	for (int item = claim_item(S, sp, live, nsplit); (item & 255) < kPlanes; item = claim_item(S, sp, live, nsplit)) {
 		const int p = item & 255, part = (item >> 8) & 15, ks = item >> 12;
 		const int r0 = part ? (int)S.split_rows[ks][part - 1] : 0, r1 = part ? (int)S.split_rows[ks][part] : 32;
@@ -883,20 +826,6 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 		const uint32_t start = incl - cnt;
 		const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
 		__syncwarp();
-		if (part == 0 && total <= 32) {
-			if (total == 0) { // only lone faces: nothing to key
-				if (any_face)
-					plane_count_one(S, p);
-				continue;
-			}
-			if (G.n == kGroupPlanes || G.total + total > 32)
-				key_group(S, G);
-			G.planes |= (uint32_t)p << (8 * G.n);
-			G.bases |= G.total << (8 * G.n);
-			G.total += total;
-			++G.n;
-			continue;
-		}
 		const int a = p / 66, s = (p % 66) >> 1, inv = p & 1;
 		Key prev{0, 0, 0};
 		uint32_t prev_b = 0, b = 0;
@@ -967,7 +896,6 @@ __device__ void plane_keys(Smem &S, const Split &sp, int live, int nsplit) {
 			plane_count_one(S, p);
 		}
 	}
-	key_group(S, G);
 }
 
 // Exact greedy scan of one plane from its masks (BlockMeshAlgo.hpp:345-477), one warp per plane.
