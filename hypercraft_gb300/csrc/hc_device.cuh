@@ -15,8 +15,8 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 32;
 constexpr int kQuadsPerMesh = 16383;       // 65,532 vertices: the uint16 split point (BlockMeshAlgo.hpp:274)
 constexpr int kMaxMeshesPerStream = 48;    // > 720,896 / 16,383
-constexpr int kMaxSplit = 4;               // face planes keyed in row parts per chunk, at most
-constexpr int kMaxParts = 4;               // row parts of a split face plane, at most
+constexpr int kMaxSplit = 16;              // face planes keyed in row parts per chunk, at most
+constexpr int kMaxParts = 8;               // row parts of a split face plane, at most
 constexpr int kPlanes = 198;               // 3 axes x 33 slices x 2 face directions
 constexpr int kSlices = 99;
 constexpr int kSegments = kPlanes + 1;     // segment 0 = custom meshes, then the planes in output order

@@ -689,26 +689,36 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t x, uint32_t *total) 
 	return incl - x;
 }
 
-// Heavy face planes (weight >= kSplitMin, the kMaxSplit heaviest) are keyed in row parts by
-// several warps (two, three or four parts by weight), so that the heaviest plane does not hold the
+// Heavy face planes (see split_heavy_planes; the kMaxSplit heaviest at most) are keyed in row parts by
+// several warps (one part per kPartWeight of weight, two to kMaxParts), so that a heavy plane does not hold the
 // key phase open; the warp that finishes last merges and counts the plane. The split rows balance
 // the weights (visible faces and complex candidates) of the parts. The row above each part after the
 // first is keyed by that part too (for the equal-below bits of that row): it reads the row's visible
 // and complex words from a copy taken here, as the part before rewrites them.
 constexpr uint32_t kSplitMin = 128;
+constexpr uint32_t kPartWeight = 96; // a split plane gets one part per this much weight (2 to kMaxParts)
 
 // After order_planes (plane weights in seg_base). Returns how many planes are split (every thread).
 __device__ int split_heavy_planes(Smem &S, int live) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t *weight = &S.seg_base[0][0];
-	// the split planes are the longest prefix of the order (at most kMaxSplit) whose weights reach
-	// kSplitMin, so that split plane k is order[k]
+	// A plane is split when it is heavy against the chunk's whole key work: weight >= kSplitMin and
+	// at least twice a warp's even share (on a chunk of many heavy planes the warps are kept busy by
+	// whole planes, and parts would only add context rows and merges). The split planes are the
+	// longest prefix of the order (at most kMaxSplit) whose weights pass, so split plane k is order[k].
 	__shared__ int s_nsplit;
-	if (threadIdx.x == 0) {
-		int k = 0;
-		while (k < kMaxSplit && k < live && weight[S.order[k]] >= kSplitMin)
-			++k;
-		s_nsplit = k;
+	if (warp == 0) {
+		uint32_t sum = 0;
+		for (int q = lane; q < live; q += 32)
+			sum += weight[S.order[q]];
+		sum = __reduce_add_sync(0xffffffffu, sum);
+		if (lane == 0) {
+			const uint32_t min_split = max(kSplitMin, 2 * sum / kWarps);
+			int k = 0;
+			while (k < kMaxSplit && k < live && weight[S.order[k]] >= min_split)
+				++k;
+			s_nsplit = k;
+		}
 	}
 	__syncthreads();
 	const int nsplit = s_nsplit;
@@ -717,7 +727,7 @@ __device__ int split_heavy_planes(Smem &S, int live) {
 		const uint32_t w = __popc(S.u.masks[p][lane][0] | S.u.masks[p][lane][1]);
 		uint32_t tot;
 		const uint32_t ex = warp_excl_scan(w, &tot);
-		const int parts = tot >= 3 * kSplitMin ? 4 : (tot >= 2 * kSplitMin ? 3 : 2);
+		const int parts = (int)min((uint32_t)kMaxParts, max(2u, (tot + kPartWeight - 1) / kPartWeight));
 		int prev = 0;
 		for (int q = 1; q < parts; ++q) { // part q starts at the row where the weight passes q / parts
 			int r = __ffs(__ballot_sync(0xffffffffu, (ex + w) * (uint32_t)parts > (uint32_t)q * tot)) - 1;
