@@ -281,34 +281,38 @@ __constant__ int16_t c_ring_off[6][8] = {
 // addition sums both channels (four 4-bit levels times four stay below 256).
 __device__ __forceinline__ uint32_t light_pair(uint32_t cell) { return (cell & 0x0fu) | ((cell & 0xf0u) << 12); }
 
+// AO of one corner by the direct-pass bits of its side, corner and other side cell and of the
+// face-front cell (index bits 0-3): 0 when both sides are blocked or the corner and the front are,
+// else 3 minus the blocked cells, at least 0 (BlockMeshAlgo.hpp:127-131). Two bits per index.
+constexpr uint32_t kAoTable = 0xe9849040u;
+
 __device__ Light4 light4(const Smem &S, int face, int x, int y, int z) {
 	const int base = cls_index(x, y, z);
 	const uint32_t cf = S.cell[base + c_front_off[face]];
-	const bool dp3 = id_direct(cf >> 8);
 	const uint32_t pf = light_pair(cf);
+	const uint32_t dp3 = (cf >> 11) & 8u; // the front cell's direct pass (class bit 6) as index bit 3
 	uint32_t ring[8];
 #pragma unroll
 	for (int i = 0; i < 8; ++i)
 		ring[i] = S.cell[base + c_ring_off[face][i]];
+	uint32_t ipm = 0, dpm = 0; // bit i: ring cell i passes light indirectly (class bit 7) / directly (bit 6)
+#pragma unroll
+	for (int i = 0; i < 8; ++i) {
+		ipm |= ((ring[i] >> 15) & 1u) << i;
+		dpm |= ((ring[i] >> 14) & 1u) << i;
+	}
+	ipm |= ipm << 8, dpm |= dpm << 8; // so that the three cells of corner 3 (6, 7, 0) are consecutive
 	Light4 r{0, 0, 0};
 #pragma unroll
-	for (int v = 0; v < 4; ++v) {
-		bool ip[3], dp[3];
-		uint32_t l[3];
-#pragma unroll
-		for (int b = 0; b < 3; ++b) { // side, corner, side (the two sides play the same part)
-			const uint32_t c = ring[(2 * v + b) & 7];
-			ip[b] = id_indirect(c >> 8);
-			dp[b] = id_direct(c >> 8);
-			l[b] = light_pair(c);
-		}
-		const int blocked = !dp[0] + !dp[1] + !dp[2] + !dp3;
-		const uint32_t ao = ((!dp[0] && !dp[2]) || (!dp[1] && !dp3)) ? 0u : (uint32_t)(3 - blocked > 0 ? 3 - blocked : 0);
+	for (int v = 0; v < 4; ++v) { // side, corner, side: ring cells 2v, 2v + 1, 2v + 2 (mod 8)
+		const uint32_t d3 = (dpm >> (2 * v)) & 7u, i3 = (ipm >> (2 * v)) & 7u;
+		const uint32_t ao = (kAoTable >> (2 * (d3 | dp3))) & 3u;
 		// the front cell, plus every light-passing side or corner cell when a side passes light
-		const bool any = ip[0] || ip[2];
-		const bool i0 = any && ip[0], i1 = any && ip[1], i2 = any && ip[2];
-		const uint32_t sum = (pf + (i0 ? l[0] : 0u) + (i1 ? l[1] : 0u) + (i2 ? l[2] : 0u)) << 2;
-		const uint32_t counter = 1u + i0 + i1 + i2;
+		const uint32_t m = (i3 & 5u) ? i3 : 0u;
+		const uint32_t sum = (pf + ((m & 1u) ? light_pair(ring[2 * v]) : 0u) + ((m & 2u) ? light_pair(ring[2 * v + 1]) : 0u) +
+		                      ((m & 4u) ? light_pair(ring[(2 * v + 2) & 7]) : 0u))
+		                     << 2;
+		const uint32_t counter = 1u + (uint32_t)__popc(m);
 		// (sum << 2) / counter in both halves: a shift for 1, 2 and 4; for 3 the multiply-high by
 		// 171 / 512, exact for every value up to 240 (Granlund and Montgomery, "Division by invariant
 		// integers using multiplication", 1994), the sun product staying below bit 16. A plain
