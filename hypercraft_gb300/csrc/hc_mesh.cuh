@@ -1096,23 +1096,25 @@ __device__ void emit_plane_quad(Smem &S, const Emit &E, BoxAcc &box, bool valid,
 		uint16_t t;
 		Light4 l;
 		face_key(S, a, s, inv, u, v, &t, &l);
-		int o[3], hv[3], wv[3];
-		to_xyz(a, s, u, v, o[0], o[1], o[2]);
-		to_xyz(a, 0, h, 0, hv[0], hv[1], hv[2]);
-		to_xyz(a, 0, 0, w, wv[0], wv[1], wv[2]);
+		// vertex word 0 (x | y << 10 | z << 20 | axis << 30, positions in 1/16 voxel) of the first
+		// corner, then the packed steps along the quad's two edges: the fields never carry into each
+		// other (positions stay within 0..512)
+		int ox, oy, oz;
+		to_xyz(a, s, u, v, ox, oy, oz);
+		const uint32_t w0 = ((uint32_t)ox << 4) | ((uint32_t)oy << 14) | ((uint32_t)oz << 24) | ((uint32_t)a << 30);
+		const int shu = a == 1 ? 20 : 10, shv = a == 0 ? 20 : 0; // U and V fields: (y, z), (z, x), (y, x)
+		const uint32_t hv = (uint32_t)h << (4 + shu), wv = (uint32_t)w << (4 + shv);
 		const bool hfirst = (inv != 0) != uv_cycle;
-		const int *du = hfirst ? hv : wv, *dv = hfirst ? wv : hv;
+		const uint32_t du = hfirst ? hv : wv, dv = hfirst ? wv : hv;
 		const uint32_t face = (uint32_t)(2 * a + inv);
+		const uint32_t w1 = ((uint32_t)(t & 0x1fffu) - 1u) | ((uint32_t)(t >> 13) << 10) | (face << 13);
+		const uint32_t p0[4] = {w0, w0 + du, w0 + du + dv, w0 + dv};
 		uint2 vt[4];
-		const int cx[4] = {o[0], o[0] + du[0], o[0] + du[0] + dv[0], o[0] + dv[0]};
-		const int cy[4] = {o[1], o[1] + du[1], o[1] + du[1] + dv[1], o[1] + dv[1]};
-		const int cz[4] = {o[2], o[2] + du[2], o[2] + du[2] + dv[2], o[2] + dv[2]};
 #pragma unroll
 		for (int c = 0; c < 4; ++c)
-			vt[c] = pack_vertex((uint32_t)cx[c] << 4, (uint32_t)cy[c] << 4, (uint32_t)cz[c] << 4, (uint32_t)a, face,
-			                    ao_get(l.ao, c), l4_get(l.sun, c), l4_get(l.torch, c), t);
-		mn[0] = (uint32_t)cx[0] << 4, mn[1] = (uint32_t)cy[0] << 4, mn[2] = (uint32_t)cz[0] << 4;
-		mx[0] = (uint32_t)cx[2] << 4, mx[1] = (uint32_t)cy[2] << 4, mx[2] = (uint32_t)cz[2] << 4;
+			vt[c] = make_uint2(p0[c], w1 | (ao_get(l.ao, c) << 16) | (l4_get(l.sun, c) << 18) | (l4_get(l.torch, c) << 24));
+		mn[0] = w0 & 1023u, mn[1] = (w0 >> 10) & 1023u, mn[2] = (w0 >> 20) & 1023u;
+		mx[0] = p0[2] & 1023u, mx[1] = (p0[2] >> 10) & 1023u, mx[2] = (p0[2] >> 20) & 1023u;
 		put_quad(S, E, st, k, g, vt, flip_of(l));
 	}
 	box_add_warp(S, box, valid, st, k / kQuadsPerMesh, mn, mx);
