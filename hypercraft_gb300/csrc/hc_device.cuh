@@ -164,6 +164,7 @@ struct Smem {
 	uint32_t split_done[kMaxSplit];
 	uint8_t split_rows[kMaxSplit][kMaxParts + 1]; // part q keys rows [rows[q], rows[q + 1])
 	uint8_t split_first[kMaxSplit + 1];           // claim index of each split plane's first part
+	uint32_t lone_planes[(kPlanes + 31) / 32];    // planes all of whose faces are lone (emitted from their masks)
 };
 
 static_assert(offsetof(Smem, u) % 16 == 0, "plane mask rows are written as 16-byte words");

@@ -34,7 +34,7 @@ __device__ __forceinline__ int claim(uint32_t *counter) {
 		j = (int)atomicAdd(counter, 1u);
 	return __shfl_sync(0xffffffffu, j, 0);
 }
-enum : int { kClaimComplex = 12, kClaimKeys = 13, kMine = 15 }; // S.misc counters
+enum : int { kClaimKeys = 13, kClaimLone = 14, kMine = 15 }; // S.misc counters
 
 // Orders the face planes by falling weight class (visible faces and complex candidates; class =
 // the weight's bit length, so the weights of a class are within a factor of two) into S.order, so
@@ -988,6 +988,8 @@ __device__ __forceinline__ uint2 get_record(const Smem &S, uint32_t j) {
 	return j < (uint32_t)kQuadBuf ? S.aux.quads[j] : S.spill[j - kQuadBuf];
 }
 
+constexpr uint32_t kLonePlaneMin = 96; // faces of an all-lone plane emitted from its masks, at least
+
 // Counts the quads of plane p (the calling warp) and keeps their records; misc[4] = records kept.
 // A row none of whose cells equals the one below, below a row of which the same holds, is
 // isolated: no quad of another row reaches it and its own quads do not grow down, so its quads are
@@ -1001,6 +1003,23 @@ __device__ void plane_count_one(Smem &S, int p) {
 	const uint32_t lt = (1u << lane) - 1u;
 	const uint32_t(*m)[4] = S.u.masks[p];
 	const uint32_t rN = m[lane][0], rE = m[lane][1], rD = m[lane][2], rT = m[lane][3];
+	{ // a plane of many faces that are all lone (a checkerboard's): its quads are its faces in
+	  // u-major order, and the emission takes them straight from the visible and transparent-pass
+	  // masks, a warp per plane, instead of from records (a few lone faces stay with the records,
+	  // whose emission is spread over the whole CTA)
+		const uint32_t rNu = __shfl_up_sync(0xffffffffu, rN, 1), rNd = __shfl_down_sync(0xffffffffu, rN, 1);
+		const uint32_t lone = rN & ~(rN << 1) & ~(rN >> 1) & ~(lane == 0 ? 0u : rNu) & ~(lane == 31 ? 0u : rNd);
+		const uint32_t all = __reduce_add_sync(0xffffffffu, __popc(rN));
+		if (all >= kLonePlaneMin && __all_sync(0xffffffffu, lone == rN)) {
+			const uint32_t tr = __reduce_add_sync(0xffffffffu, __popc(rN & rT));
+			if (lane == 0) {
+				S.seg_cnt[0][1 + p] = all - tr;
+				S.seg_cnt[1][1 + p] = tr;
+				atomicOr(&S.lone_planes[p >> 5], 1u << (p & 31));
+			}
+			return;
+		}
+	}
 	const uint32_t rDup = __shfl_up_sync(0xffffffffu, rD, 1);
 	const bool iso = rD == 0 && (lane == 0 || rDup == 0);
 	const uint32_t icont = rN & (rN << 1) & (rE << 1); // bit v continues the run of v - 1
@@ -1128,6 +1147,47 @@ __device__ __forceinline__ void emit_record(Smem &S, const Emit &E, BoxAcc &box,
 	                valid ? S.seg_base[2][1 + p] + li : 0u);
 }
 
+// Emits the quads of a plane all of whose faces are lone (the calling warp): each face is a quad of
+// its own, its index among the plane's quads is its index among the plane's faces (u-major) and
+// its stream the face's transparent-pass bit. Faces are taken in batches of whole rows, one per lane.
+__device__ void emit_lone_plane(Smem &S, const Emit &E, BoxAcc &box, int p) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t(*m)[4] = S.u.masks[p];
+	const uint32_t rN = m[lane][0], rT = m[lane][3] & m[lane][0];
+	const uint32_t cnt = __popc(rN), incl = row_scan(cnt), start = incl - cnt;
+	const uint32_t tcnt = __popc(rT), tstart = row_scan(tcnt) - tcnt;
+	const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+	const uint32_t base_all = S.seg_base[2][1 + p], base_st[2] = {S.seg_base[0][1 + p], S.seg_base[1][1 + p]};
+	const uint32_t upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+	uint32_t b = 0;
+	int ub = 0;
+	while (b < total) {
+		// rows [ub, ue) whose faces fit in 32 lanes from index b (as in the key pass)
+		const uint32_t over = __ballot_sync(0xffffffffu, lane >= ub && incl > b + 32);
+		const int ue = over ? __ffs(over) - 1 : 32;
+		const uint32_t be = __shfl_sync(0xffffffffu, start, ue & 31);
+		const uint32_t bend = ue < 32 ? be : total;
+		const uint32_t f = b + lane;
+		const bool has = f < bend;
+		const bool rin = lane >= ub && lane < ue && cnt > 0;
+		const uint32_t M = __reduce_or_sync(0xffffffffu, rin ? 1u << (start - b) : 0u);
+		if (rin)
+			S.row_of[warp][start - b] = (uint8_t)lane;
+		__syncwarp();
+		const int u = has ? S.row_of[warp][31 - __clz(M & upto)] : 0;
+		__syncwarp();
+		const uint32_t su = __shfl_sync(0xffffffffu, start, u), Nu = __shfl_sync(0xffffffffu, rN, u);
+		const uint32_t Tu = __shfl_sync(0xffffffffu, rT, u), tsu = __shfl_sync(0xffffffffu, tstart, u);
+		const int v = has ? nth_set_bit(Nu, f - su) : 0;
+		const int st = (int)((Tu >> v) & 1u);
+		const uint32_t tb = tsu + __popc(Tu & ((1u << v) - 1u)); // transparent faces before this one
+		const uint32_t lk = st ? tb : f - tb;
+		emit_plane_quad(S, E, box, has, p, u, v, 1, 1, st, has ? base_st[st] + lk : 0u, has ? base_all + f : 0u);
+		b = bend;
+		ub = ue;
+	}
+}
+
 // Emits the plane quads this CTA owns. Normally plane_count_one kept all their records; otherwise
 // this CTA's quads are taken in windows of kQuadBuf (its planes in the order it took them, each
 // plane's quads in order), the planes overlapping a window merge again to stage that window's
@@ -1141,6 +1201,23 @@ __device__ void planes_emit(Smem &S, const Emit &E, const Split &sp) {
 		for (uint32_t j0 = (uint32_t)warp * 32; j0 < n; j0 += kThreads) {
 			const uint32_t j = j0 + lane;
 			emit_record(S, E, box, j < n, j < n ? get_record(S, j) : make_uint2(0, 0));
+		}
+		// then the planes whose faces are all lone, one warp per plane
+		uint32_t any_lone = 0;
+#pragma unroll
+		for (int i = 0; i < (kPlanes + 31) / 32; ++i)
+			any_lone |= S.lone_planes[i];
+		const int n_mine = any_lone ? (int)S.misc[kMine] : 0;
+		for (;;) {
+			int j = 0;
+			if (lane == 0)
+				j = (int)atomicAdd(&S.misc[kClaimLone], 1u);
+			j = __shfl_sync(0xffffffffu, j, 0);
+			if (j >= n_mine)
+				break;
+			const int p = S.mine[j];
+			if ((S.lone_planes[p >> 5] >> (p & 31)) & 1u)
+				emit_lone_plane(S, E, box, p);
 		}
 		box_flush(S, box);
 		return;
@@ -1311,7 +1388,9 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 		S.seg_cnt[i / (kSegments + 1)][i % (kSegments + 1)] = 0;
 	if (tid < 6) // claim counters, records kept, records overflow; the stage's barriers (and, in a
 	             // cluster, the relight's) order this before any CTA's plane phases
-		S.misc[tid < 4 ? kClaimComplex + tid : tid] = 0;
+		S.misc[tid < 4 ? 12 + tid : tid] = 0;
+	if (tid < (kPlanes + 31) / 32)
+		S.lone_planes[tid] = 0;
 	if (tid == 0) {
 		S.spill = A.spill ? A.spill + (size_t)blockIdx.x * kSpillRecs : nullptr;
 		S.spill_cap = A.spill ? kSpillRecs : 0u;
