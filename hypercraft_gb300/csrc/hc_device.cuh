@@ -165,6 +165,8 @@ struct Smem {
 	uint8_t split_rows[kMaxSplit][kMaxParts + 1]; // part q keys rows [rows[q], rows[q + 1])
 	uint8_t split_first[kMaxSplit + 1];           // claim index of each split plane's first part
 	uint32_t lone_planes[(kPlanes + 31) / 32];    // planes all of whose faces are lone (emitted from their masks)
+	int8_t lvl_slot[32];  // per light-level plane of the chunk (channel * 15 + level - 1): its copy in the staging scratch, or -1
+	int8_t lvl_plane[16]; // ... and per copy, its plane
 };
 
 static_assert(offsetof(Smem, u) % 16 == 0, "plane mask rows are written as 16-byte words");

@@ -217,6 +217,14 @@ __device__ __forceinline__ void put_quad(Smem &S, const Emit &E, int st, uint32_
 // where there are planes, else built by ballots). Returns true when the chunk can produce no quad:
 // every inner block has no texture and no custom mesh, or every inner block and every block of the
 // six adjacent layers is an opaque full cube; has_custom: some inner block has a custom mesh.
+// The staging scratch (the plane-mask memory): the chunk's 32 KB of class ids, the 132 apron rows
+// (32 bytes each), then as many of the chunk's stored level planes (4 KB each) as fit.
+constexpr int kStagedLevelOff = 32768 + 32 * (kCls * kCls - kChunk * kChunk);
+constexpr int kStagedLevels = (int)((sizeof(Smem::u) - kStagedLevelOff) / (kPlaneWords * 4)) < 2 * kLevels
+                                  ? (int)((sizeof(Smem::u) - kStagedLevelOff) / (kPlaneWords * 4))
+                                  : 2 * kLevels;
+static_assert(kStagedLevelOff % 16 == 0 && kStagedLevels >= 1 && kStagedLevels <= 16, "level copies fit the scratch");
+
 __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	constexpr int kRows = kCls * kCls, kBatch = 12; // 1156 rows; 12 in flight per warp
@@ -225,8 +233,22 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 	if (S.pln[26]) {
 		// The blank test first, from the layer summaries of the chunk and its six face neighbours
 		// (one warp, 32 words each), so a blank chunk stages nothing.
-		__shared__ uint32_t s_blank, s_custom;
+		__shared__ uint32_t s_blank, s_custom, s_staged;
 		if (warp == 0) {
+			if (S.lvl[26]) { // the chunk's stored (non-uniform) level planes, the first kStagedLevels of them staged
+				const uint32_t fl = lane < 2 * kLevels ? S.lfl[26][lane / kLevels] : 0u;
+				const int t = lane % kLevels + 1;
+				const bool stored = lane < 2 * kLevels && !level_empty(fl, t) && !level_full(fl, t);
+				const uint32_t m = __ballot_sync(0xffffffffu, stored);
+				const int slot = __popc(m & ((1u << lane) - 1u));
+				const bool staged = stored && slot < kStagedLevels;
+				if (lane < 2 * kLevels)
+					S.lvl_slot[lane] = staged ? (int8_t)slot : (int8_t)-1;
+				if (staged)
+					S.lvl_plane[slot] = (int8_t)lane;
+				if (lane == 0)
+					s_staged = min(__popc(m), kStagedLevels);
+			}
 			const uint32_t mine = __ldg(S.pln[26] + kPlaneLayerOff + lane);
 			const uint32_t xm = __ldg(S.pln[nb_index(-1, 0, 0)] + kPlaneLayerOff + lane);
 			const uint32_t xp = __ldg(S.pln[nb_index(kChunk, 0, 0)] + kPlaneLayerOff + lane);
@@ -262,14 +284,26 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 			asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 32768 + 32 * a + 16 * half), "l"(row)
 			             : "memory");
 		}
+		// With the batch light pass's level planes, up to kStagedLevels stored level planes of the
+		// chunk itself (4 KB each) follow the apron rows, copied the same way.
+		const bool lit = S.lvl[26] != nullptr;
+		if (lit) {
+			const uint32_t nw = s_staged * (kPlaneWords / 4);
+			for (uint32_t i = threadIdx.x; i < nw; i += kThreads) {
+				const uint32_t slot = i / (kPlaneWords / 4), q = i % (kPlaneWords / 4);
+				const uint32_t *p = S.lvl[26] + (size_t)S.lvl_plane[slot] * kPlaneWords + 4 * q;
+				asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + kStagedLevelOff + 16 * i), "l"(p)
+				             : "memory");
+			}
+		}
 		asm volatile("cp.async.commit_group;" ::: "memory");
 		for (int i = threadIdx.x; i < 256; i += kThreads)
 			S.classes[i] = T.classes[i];
-		// With the batch light pass's level planes, each row's light is decoded after the row bits
-		// below (its loads overlapping the copies still in flight) and written together with the
-		// row's class ids as whole cells; otherwise the class ids go in with light 0, for the
+		// With the batch light pass's level planes, the light of the apron rows and of the x-edge
+		// pieces is decoded after the row bits below (its loads overlapping the copies still in
+		// flight), that of the chunk's own rows after the copies, and each row is written together
+		// with its class ids as whole cells; otherwise the class ids go in with light 0, for the
 		// relight to raise.
-		const bool lit = S.lvl[26] != nullptr;
 		uint8_t *const hi = reinterpret_cast<uint8_t *>(S.cell) + 1;
 		// First, one thread per row of [-1, 32]^2: the opaque-cube and blank bits of the row from
 		// its chunk's planes with the x = -1 and x = 32 bits from the x neighbours' (bit x + 1), and
@@ -291,32 +325,30 @@ __device__ bool stage_classes(Smem &S, const DevTables &T, bool &has_custom) {
 				S.cell[row * kCls + kCls - 1] = (uint16_t)(e1 << 8);
 			}
 		}
-		// the light of each row item is decoded now (its level-plane loads overlapping the copies still in flight)
-		// and kept in registers until the row's class ids have arrived; edge pieces are written now
-		constexpr int kLightItems = kLt * kLt + 2 * kLt * 3;
-		static_assert(kLightItems <= 2 * kThreads, "two light items per thread at most");
-		uint64_t lrow[2][4];
-		bool has_row[2] = {false, false};
-		if (lit) {
-#pragma unroll
-			for (int k = 0; k < 2; ++k) { // both items' level loads in flight together
-				const int it = threadIdx.x + k * kThreads;
-				if (it < kLightItems)
-					has_row[k] = light_item(S, it, lrow[k]);
+		// the light of apron row a (thread a < 132) or edge piece threadIdx.x - 132 is decoded now and
+		// the apron row's kept in registers until its class ids have arrived; edge pieces are written now
+		constexpr int kOtherItems = kApronRows + 2 * kLt * 3;
+		static_assert(kOtherItems <= kThreads && kChunk * kChunk == kThreads, "one item of each kind per thread");
+		uint64_t lrow[4];
+		int arow = -1;
+		if (lit && threadIdx.x < kOtherItems) {
+			int it = kLt * kLt + (threadIdx.x - kApronRows);
+			if (threadIdx.x < kApronRows) {
+				const int a = threadIdx.x;
+				const int y = a < 34 ? -1 : (a < 68 ? kChunk : (a - 68) >> 1);
+				const int z = a < 34 ? a - 1 : (a < 68 ? a - 35 : (((a - 68) & 1) ? kChunk : -1));
+				it = arow = (y + 1) * kCls + (z + 1);
 			}
+			light_item(S, it, lrow);
 		}
 		asm volatile("cp.async.wait_group 0;" ::: "memory");
 		__syncthreads();
-		if (lit) { // light and class id of the cells x in [0, 32) of each row item, as whole cells
-#pragma unroll
-			for (int k = 0; k < 2; ++k) {
-				if (!has_row[k])
-					continue;
-				const int row = threadIdx.x + k * kThreads, y = row / kCls - 1, z = row % kCls - 1;
-				const bool inner = (unsigned)y < (unsigned)kChunk && (unsigned)z < (unsigned)kChunk;
-				const int a = y < 0 ? z + 1 : (y >= kChunk ? 35 + z : 68 + 2 * y + (z >= kChunk)); // apron row
-				write_row_cells(S, row, lrow[k], own + (inner ? (y * kChunk + z) * kChunk : 32768 + 32 * a));
-			}
+		if (lit) { // light and class id of the cells x in [0, 32) of each row, as whole cells
+			if (arow >= 0)
+				write_row_cells(S, arow, lrow, own + 32768 + 32 * threadIdx.x);
+			const int y = threadIdx.x >> 5, z = threadIdx.x & 31; // the chunk's own row of this thread
+			light_own_row(S, y, z, reinterpret_cast<const uint32_t *>(own + kStagedLevelOff), lrow);
+			write_row_cells(S, (y + 1) * kCls + z + 1, lrow, own + (y * kChunk + z) * kChunk);
 			__syncthreads();
 			return false;
 		}
@@ -1386,9 +1418,9 @@ __device__ void mesh_chunk_cta(Smem &S, const DevTables &T, const Arena &A, uint
 	}
 	for (int i = tid; i < 2 * (kSegments + 1); i += kThreads)
 		S.seg_cnt[i / (kSegments + 1)][i % (kSegments + 1)] = 0;
-	if (tid < 6) // claim counters, records kept, records overflow; the stage's barriers (and, in a
-	             // cluster, the relight's) order this before any CTA's plane phases
-		S.misc[tid < 4 ? 12 + tid : tid] = 0;
+	if (tid < 5) // the claim counters, records kept, records overflow; the stage's barriers (and,
+	             // in a cluster, the relight's) order this before any CTA's plane phases
+		S.misc[tid < 3 ? kClaimKeys + tid : tid + 1] = 0; // misc[13..15], misc[4..5]
 	if (tid < (kPlanes + 31) / 32)
 		S.lone_planes[tid] = 0;
 	if (tid == 0) {

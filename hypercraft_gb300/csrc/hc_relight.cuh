@@ -395,8 +395,8 @@ __device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hg
 constexpr int kLevels = 15;
 constexpr size_t kLevelSlotWords = (size_t)2 * kLevels * kPlaneWords; // per chunk: 2 channels x 15 levels
 constexpr size_t kEdgeSlotWords = (size_t)2 * kLevels * 2 * 32;       // per chunk: x = 0 and x = 31 bits
-constexpr int kLightThreads = 128;                                     // one block per chunk
-constexpr int kLightRows = kPlaneWords / kLightThreads;                // rows per thread
+constexpr int kLightWarps = 4;                                         // chunks per block, one warp each
+constexpr int kLightThreads = 32 * kLightWarps;
 
 struct LightPass {
 	const int32_t *slots;   // batch chunk -> pool slot
@@ -442,206 +442,208 @@ __device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
 	           mux(b[2], mux(b[1], s[6], s[4]), mux(b[1], s[2], s[0])));
 }
 
-// Level t of every batch chunk, one block per chunk: the chunk's level t + 1 rows and the rows and
-// edge bits of its six face neighbours that touch it are staged in shared memory with coalesced
-// loads (the chunk's own rows are requested before its neighbour list arrives), then each thread
-// dilates kLightRows rows of both channels. Also writes the row edge bits that the x neighbours
-// read at the next level, and the plane's uniform bits (LightPass::flags). A channel whose level
-// follows from level t + 1 without computing (see kFlag*) is skipped: a chunk of sunlit air far
-// from any emitter costs one flag word per level.
-__global__ void __launch_bounds__(kLightThreads, 16) k_light_level(LightPass L, DevTables T, int t) {
-	__shared__ __align__(16) uint32_t prev[2][kPlaneWords];
-	__shared__ uint32_t side[2][6][32]; // per channel: -x hi edge, +x lo edge, -y rows, +y rows, -z rows, +z rows
-	__shared__ int s_nb[6];
-	__shared__ int32_t s_slot;
-	__shared__ uint32_t s_fl[7][2]; // level t + 1 flags: the six face neighbours, then the chunk
-	__shared__ uint32_t s_run;      // bit c: channel c is computed at this level
-	const int tid = threadIdx.x, lane = tid & 31;
-	const int i = blockIdx.x;
+// Level t of every batch chunk, one warp per chunk (lane = z): the warp walks the chunk's 32 y
+// layers, keeping the level t + 1 rows of layers y - 1, y and y + 1 in registers, and dilates both
+// channels of each layer with shifts (x), shuffles (z) and the neighbouring layers (y). The face
+// neighbours' touching rows and edge bits are loaded once, one word per lane. Also writes the row
+// edge bits that the x neighbours read at the next level, and the plane's uniform bits
+// (LightPass::flags). A channel whose level follows from level t + 1 without computing (see kFlag*)
+// is skipped: a chunk of sunlit air far from any emitter costs one flag word per level. No block
+// barrier: the warps of a block are independent chunks.
+__global__ void __launch_bounds__(kLightThreads, 8) k_light_level(LightPass L, DevTables T, int t) {
+	constexpr uint32_t kAll = 0xffffffffu;
+	const int lane = threadIdx.x & 31;
+	const uint32_t i = blockIdx.x * kLightWarps + (threadIdx.x >> 5);
+	if (i >= L.n) // the whole warp
+		return;
+	// lanes 0-5: the face neighbours; lane 6: the pool slot; lanes 8-9: the flags; lanes 10-11: the
+	// near bits (flags and near bits from level t + 1)
+	int32_t v1 = -1;
+	if (lane < 6)
+		v1 = __ldg(L.nb6 + 6 * (size_t)i + lane);
+	else if (lane == 6)
+		v1 = __ldg(L.slots + i);
+	else if (t < kLevels && lane >= 8 && lane < 10)
+		v1 = (int32_t)__ldg(L.flags + 2 * (size_t)i + (lane - 8));
+	else if (t < kLevels && lane >= 10 && lane < 12)
+		v1 = (int32_t)__ldg(L.near + 2 * (size_t)i + (lane - 10));
+	const int slot = __shfl_sync(kAll, v1, 6);
+	// lane l < 14: channel l / 7 and face l % 7 (6 = the chunk itself), for the near bits it sets
+	const int nb7 = __shfl_sync(kAll, v1, lane % 7 < 6 ? lane % 7 : 0);
+	const int near_nb = lane % 7 < 6 ? nb7 : (int)i;
+	const uint32_t *P = L.planes + (size_t)slot * kPlaneStride;
+	uint32_t *const lev = L.levels + (size_t)i * kLevelSlotWords;
+	uint32_t *const edg = L.edges + (size_t)i * kEdgeSlotWords;
 	if (t == kLevels) { // the seeds: sunlit cells, emitters of level 15 (uniform planes are not stored)
-		if (tid == 0)
-			s_slot = __ldg(L.slots + i);
-		__syncthreads();
-		const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
-		uint32_t s[kLightRows][2];
-		bool any[2] = {false, false}, all[2] = {true, true}, low = false;
-#pragma unroll
-		for (int k = 0; k < kLightRows; ++k) {
-			const int r = tid + k * kLightThreads;
-			s[k][0] = __ldg(P + kPlaneSun * kPlaneWords + r);
-			s[k][1] = __ldg(P + kPlaneT15 * kPlaneWords + r);
-			low |= ((__ldg(P + kPlaneLowOff + (r >> 5)) >> (r & 31)) & 1u) != 0;
-#pragma unroll
-			for (int c = 0; c < 2; ++c)
-				any[c] |= s[k][c] != 0, all[c] &= s[k][c] == 0xffffffffu;
+		const uint32_t low = __ldg(P + kPlaneLowOff + lane);
+		bool any[2] = {false, false}, all[2] = {true, true};
+#pragma unroll 8
+		for (int y = 0; y < 32; ++y) {
+			const uint32_t s0 = __ldg(P + kPlaneSun * kPlaneWords + y * 32 + lane);
+			const uint32_t s1 = __ldg(P + kPlaneT15 * kPlaneWords + y * 32 + lane);
+			any[0] |= s0 != 0, all[0] &= s0 == kAll;
+			any[1] |= s1 != 0, all[1] &= s1 == kAll;
 		}
 		uint32_t fl[2];
 		bool store[2];
 #pragma unroll
 		for (int c = 0; c < 2; ++c) {
-			const bool a = __syncthreads_or(any[c]), f = __syncthreads_and(all[c]);
+			const bool a = __any_sync(kAll, any[c]), f = __all_sync(kAll, all[c]);
 			fl[c] = (a ? 0u : 1u << (kLevels - 1)) | (f ? 1u << (kFlagFull + kLevels - 1) : 0u);
 			store[c] = a && !f;
 		}
-		fl[1] |= __syncthreads_or(low) ? kFlagLowEmitters : 0u;
+		fl[1] |= __any_sync(kAll, low != 0) ? kFlagLowEmitters : 0u;
+		if (store[0] || store[1]) { // the rows again (in L1 now), stored with their edge bits
+			uint32_t elo[2] = {0u, 0u}, ehi[2] = {0u, 0u};
+#pragma unroll 8
+			for (int y = 0; y < 32; ++y) {
 #pragma unroll
-		for (int k = 0; k < kLightRows; ++k) {
-			const int r = tid + k * kLightThreads;
+				for (int c = 0; c < 2; ++c) {
+					if (!store[c])
+						continue;
+					const uint32_t s = __ldg(P + (c ? kPlaneT15 : kPlaneSun) * kPlaneWords + y * 32 + lane);
+					lev[(size_t)(c * kLevels + kLevels - 1) * kPlaneWords + y * 32 + lane] = s;
+					const uint32_t lo = __ballot_sync(kAll, s & 1u), hi = __ballot_sync(kAll, s >> 31);
+					if (lane == y)
+						elo[c] = lo, ehi[c] = hi;
+				}
+			}
 #pragma unroll
 			for (int c = 0; c < 2; ++c) {
 				if (!store[c])
 					continue;
-				L.levels[(size_t)i * kLevelSlotWords + (size_t)(c * kLevels + kLevels - 1) * kPlaneWords + r] = s[k][c];
-				const uint32_t lo = __ballot_sync(0xffffffffu, s[k][c] & 1u), hi = __ballot_sync(0xffffffffu, s[k][c] >> 31);
-				if (lane == 0) {
-					uint32_t *e = L.edges + (size_t)i * kEdgeSlotWords + (size_t)(c * kLevels + kLevels - 1) * 64;
-					e[r >> 5] = lo;
-					e[32 + (r >> 5)] = hi;
-				}
+				uint32_t *e = edg + (size_t)(c * kLevels + kLevels - 1) * 64;
+				e[lane] = elo[c];
+				e[32 + lane] = ehi[c];
 			}
 		}
-		if (tid < 2)
-			L.flags[2 * (size_t)i + tid] = fl[tid];
-		if (tid < 14) { // a non-empty level 15 may light this chunk and its face neighbours at level 14
-			const int c = tid / 7, f = tid % 7;
-			const int nb = f < 6 ? __ldg(L.nb6 + 6 * i + f) : i;
-			if (nb >= 0 && !level_empty(fl[c], kLevels))
-				atomicOr(L.near + 2 * (size_t)nb + c, 1u << (kLevels - 2));
+		if (lane < 2)
+			L.flags[2 * (size_t)i + lane] = lane ? fl[1] : fl[0];
+		if (lane < 14) { // a non-empty level 15 may light this chunk and its face neighbours at level 14
+			const int c = lane / 7;
+			if (near_nb >= 0 && !level_empty(c ? fl[1] : fl[0], kLevels))
+				atomicOr(L.near + 2 * (size_t)near_nb + c, 1u << (kLevels - 2));
 		}
 		return;
 	}
-	__shared__ uint32_t s_near[2];
-	if (tid < 6)
-		s_nb[tid] = __ldg(L.nb6 + 6 * i + tid);
-	if (tid == 6)
-		s_slot = __ldg(L.slots + i);
-	if (tid < 2) {
-		s_fl[6][tid] = __ldg(L.flags + 2 * (size_t)i + tid);
-		s_near[tid] = __ldg(L.near + 2 * (size_t)i + tid);
-	}
-	__syncthreads();
-	if (tid == 0) { // which channels follow from level t + 1 without computing
-		uint32_t run = 0;
+	const uint32_t own[2] = {(uint32_t)__shfl_sync(kAll, v1, 8), (uint32_t)__shfl_sync(kAll, v1, 9)};
+	const uint32_t nr[2] = {(uint32_t)__shfl_sync(kAll, v1, 10), (uint32_t)__shfl_sync(kAll, v1, 11)};
+	// which channels follow from level t + 1 without computing: full stays full; empty stays empty
+	// when no face neighbour had light at level t + 1 and no emitter seeds level t
+	uint32_t run = 0;
 #pragma unroll
-		for (int c = 0; c < 2; ++c) {
-			const uint32_t own = s_fl[6][c];
-			// full stays full; empty stays empty when no face neighbour had light at level t + 1 and no
-			// emitter seeds level t
-			const bool full = level_full(own, t + 1);
-			const bool trivial = full || (level_empty(own, t + 1) && !((s_near[c] >> (t - 1)) & 1u) &&
-			                              !(c == 1 && (own & kFlagLowEmitters)));
-			if (trivial)
-				atomicOr(L.flags + 2 * (size_t)i + c, full ? 1u << (kFlagFull + t - 1) : 1u << (t - 1));
-			else
-				run |= 1u << c;
-		}
-		s_run = run;
+	for (int c = 0; c < 2; ++c) {
+		const bool full = level_full(own[c], t + 1);
+		const bool trivial = full || (level_empty(own[c], t + 1) && !((nr[c] >> (t - 1)) & 1u) &&
+		                              !(c == 1 && (own[c] & kFlagLowEmitters)));
+		if (!trivial)
+			run |= 1u << c;
+		else if (lane == c)
+			atomicOr(L.flags + 2 * (size_t)i + c, full ? 1u << (kFlagFull + t - 1) : 1u << (t - 1));
 	}
-	__syncthreads();
-	const uint32_t run = s_run;
 	// a full plane at level t (it stays full) lights this chunk and its face neighbours at level t - 1
-	if (t > 1 && tid < 14) {
-		const int c = tid / 7, f = tid % 7;
-		const int nb = f < 6 ? s_nb[f] : i;
-		if (nb >= 0 && !((run >> c) & 1u) && level_full(s_fl[6][c], t + 1))
-			atomicOr(L.near + 2 * (size_t)nb + c, 1u << (t - 2));
+	if (t > 1 && lane < 14) {
+		const int c = lane / 7;
+		if (near_nb >= 0 && !((run >> c) & 1u) && level_full(c ? own[1] : own[0], t + 1))
+			atomicOr(L.near + 2 * (size_t)near_nb + c, 1u << (t - 2));
 	}
 	if (!run)
 		return;
-	if (tid < 12) { // the neighbours' flags (a missing neighbour is dark: empty)
-		const int f = tid >> 1, c = tid & 1, nb = s_nb[f];
-		s_fl[f][c] = nb >= 0 ? __ldg(L.flags + 2 * (size_t)nb + c) : 0xffffu;
-	}
-	const uint32_t *P = L.planes + (size_t)s_slot * kPlaneStride;
-	constexpr int kQ = kPlaneWords / 4 / kLightThreads; // uint4 of one channel per thread
+	// lanes 0-11: the neighbours' level t + 1 flags, face lane / 2, channel lane % 2 (a missing
+	// neighbour is dark: empty)
+	const int nbq = __shfl_sync(kAll, v1, lane < 12 ? lane >> 1 : 0);
+	uint32_t nfl = 0xffffu;
+	if (lane < 12 && nbq >= 0)
+		nfl = __ldg(L.flags + 2 * (size_t)nbq + (lane & 1));
+	int nb[6];
 #pragma unroll
-	for (int c = 0; c < 2; ++c) { // the chunk's own level t + 1 rows, meanwhile
-		if (!((run >> c) & 1u))
-			continue;
-		const uint32_t own = s_fl[6][c];
-#pragma unroll
-		for (int q = 0; q < kQ; ++q) {
-			const int o = tid + q * kLightThreads;
-			uint4 v;
-			if (level_empty(own, t + 1))
-				v = make_uint4(0u, 0u, 0u, 0u);
-			else if (level_full(own, t + 1))
-				v = make_uint4(~0u, ~0u, ~0u, ~0u);
-			else
-				v = __ldg(reinterpret_cast<const uint4 *>(level_plane(L, i, c, t + 1)) + o);
-			reinterpret_cast<uint4 *>(prev[c])[o] = v;
-		}
-	}
-	__syncthreads();
+	for (int f = 0; f < 6; ++f)
+		nb[f] = __shfl_sync(kAll, v1, f);
+	// per channel, lane k: x = -1 bits over z of layer k, x = 32 bits, the y = -1 and y = 32 rows
+	// at z = k, the z = -1 and z = 32 rows of layer k
+	uint32_t sxm[2], sxp[2], sym[2], syp[2], szm[2], szp[2];
 #pragma unroll
 	for (int c = 0; c < 2; ++c) {
+		uint32_t fl[6];
+#pragma unroll
+		for (int f = 0; f < 6; ++f)
+			fl[f] = __shfl_sync(kAll, nfl, 2 * f + c);
+		sxm[c] = sxp[c] = sym[c] = syp[c] = szm[c] = szp[c] = 0u;
 		if (!((run >> c) & 1u))
 			continue;
-		for (int j = tid; j < 6 * 32; j += kLightThreads) {
-			const int f = j >> 5, k = j & 31, nb = s_nb[f];
-			uint32_t v = 0;
-			if (nb >= 0) {
-				const uint32_t fl = s_fl[f][c];
-				if (f == 0)
-					v = level_word(fl, t + 1, level_edges(L, nb, c, t + 1) + 32 + k); // x = 31 bits of the -x neighbour
-				else if (f == 1)
-					v = level_word(fl, t + 1, level_edges(L, nb, c, t + 1) + k); // x = 0 bits of the +x neighbour
-				else if (f == 2)
-					v = level_word(fl, t + 1, level_plane(L, nb, c, t + 1) + 31 * 32 + k); // its y = 31 row at z = k
-				else if (f == 3)
-					v = level_word(fl, t + 1, level_plane(L, nb, c, t + 1) + k); // y = 0, z = k
-				else if (f == 4)
-					v = level_word(fl, t + 1, level_plane(L, nb, c, t + 1) + k * 32 + 31); // z = 31 row at y = k
-				else
-					v = level_word(fl, t + 1, level_plane(L, nb, c, t + 1) + k * 32); // z = 0, y = k
-			}
-			side[c][f][k] = v;
-		}
+		if (nb[0] >= 0)
+			sxm[c] = level_word(fl[0], t + 1, level_edges(L, nb[0], c, t + 1) + 32 + lane);
+		if (nb[1] >= 0)
+			sxp[c] = level_word(fl[1], t + 1, level_edges(L, nb[1], c, t + 1) + lane);
+		if (nb[2] >= 0)
+			sym[c] = level_word(fl[2], t + 1, level_plane(L, nb[2], c, t + 1) + 31 * 32 + lane);
+		if (nb[3] >= 0)
+			syp[c] = level_word(fl[3], t + 1, level_plane(L, nb[3], c, t + 1) + lane);
+		if (nb[4] >= 0)
+			szm[c] = level_word(fl[4], t + 1, level_plane(L, nb[4], c, t + 1) + lane * 32 + 31);
+		if (nb[5] >= 0)
+			szp[c] = level_word(fl[5], t + 1, level_plane(L, nb[5], c, t + 1) + lane * 32);
 	}
-	uint32_t pass[kLightRows], lows[kLightRows], s[kLightRows][2];
+	// the chunk's own level t + 1 rows: stored, or a constant (a computed channel's level t + 1 is
+	// stored or empty)
+	const uint32_t *src[2] = {level_plane(L, i, 0, t + 1), level_plane(L, i, 1, t + 1)};
+	const bool stored[2] = {!level_empty(own[0], t + 1) && !level_full(own[0], t + 1),
+	                        !level_empty(own[1], t + 1) && !level_full(own[1], t + 1)};
+	const uint32_t cst[2] = {level_full(own[0], t + 1) ? kAll : 0u, level_full(own[1], t + 1) ? kAll : 0u};
+	const uint32_t lows = (run & 2u) ? __ldg(P + kPlaneLowOff + lane) : 0u; // lane y: low-emitter rows of layer y
+	uint32_t up[2], me[2];
 #pragma unroll
-	for (int k = 0; k < kLightRows; ++k) {
-		const int r = tid + k * kLightThreads;
-		pass[k] = __ldg(P + kPlanePass * kPlaneWords + r);
-		lows[k] = (run & 2u) ? __ldg(P + kPlaneLowOff + (r >> 5)) : 0u;
+	for (int c = 0; c < 2; ++c) {
+		up[c] = sym[c];
+		me[c] = stored[c] ? __ldg(src[c] + lane) : cst[c];
 	}
-	__syncthreads();
+	uint32_t elo[2] = {0u, 0u}, ehi[2] = {0u, 0u};
 	bool any[2] = {false, false}, all[2] = {true, true};
+	constexpr int kBatch = 8; // layers whose rows are requested together
+	for (int y0 = 0; y0 < 32; y0 += kBatch) {
+		uint32_t pass[kBatch], next[2][kBatch];
 #pragma unroll
-	for (int k = 0; k < kLightRows; ++k) {
-		const int r = tid + k * kLightThreads, y = r >> 5, z = r & 31;
+		for (int j = 0; j < kBatch; ++j) {
+			const int y = y0 + j;
+			pass[j] = __ldg(P + kPlanePass * kPlaneWords + y * 32 + lane);
 #pragma unroll
-		for (int c = 0; c < 2; ++c) {
-			if (!((run >> c) & 1u))
-				continue;
-			const uint32_t me = prev[c][r];
-			uint32_t d = (me << 1) | (me >> 1);
-			d |= (side[c][0][r >> 5] >> (r & 31)) & 1u;
-			d |= ((side[c][1][r >> 5] >> (r & 31)) & 1u) << 31;
-			d |= y > 0 ? prev[c][r - 32] : side[c][2][z];
-			d |= y < 31 ? prev[c][r + 32] : side[c][3][z];
-			d |= z > 0 ? prev[c][r - 1] : side[c][4][y];
-			d |= z < 31 ? prev[c][r + 1] : side[c][5][y];
-			s[k][c] = me | (pass[k] & d);
-		}
-		if ((lows[k] >> (r & 31)) & 1u) { // emitters below level 15 in this row
-			const uint16_t *row = L.blocks + (size_t)s_slot * 32768 + r * 32;
-			for (int x = 0; x < 32; ++x)
-				if (T.classes[T.class_of[row[x]]].light >= t)
-					s[k][1] |= 1u << x;
+			for (int c = 0; c < 2; ++c)
+				next[c][j] = y < 31 ? (stored[c] ? __ldg(src[c] + (y + 1) * 32 + lane) : cst[c]) : syp[c];
 		}
 #pragma unroll
-		for (int c = 0; c < 2; ++c) {
-			if (!((run >> c) & 1u))
-				continue;
-			any[c] |= s[k][c] != 0, all[c] &= s[k][c] == 0xffffffffu;
-			uint32_t *out = L.levels + (size_t)i * kLevelSlotWords + (size_t)(c * kLevels + t - 1) * kPlaneWords;
-			out[r] = s[k][c];
-			const uint32_t lo = __ballot_sync(0xffffffffu, s[k][c] & 1u), hi = __ballot_sync(0xffffffffu, s[k][c] >> 31);
-			if (lane == 0) {
-				uint32_t *e = L.edges + (size_t)i * kEdgeSlotWords + (size_t)(c * kLevels + t - 1) * 64;
-				e[r >> 5] = lo;
-				e[32 + (r >> 5)] = hi;
+		for (int j = 0; j < kBatch; ++j) {
+			const int y = y0 + j;
+			const uint32_t lowy = __shfl_sync(kAll, lows, y);
+#pragma unroll
+			for (int c = 0; c < 2; ++c) {
+				if (!((run >> c) & 1u))
+					continue;
+				const uint32_t m = me[c], dn = next[c][j];
+				const uint32_t xm = __shfl_sync(kAll, sxm[c], y), xp = __shfl_sync(kAll, sxp[c], y);
+				const uint32_t zm = __shfl_sync(kAll, szm[c], y), zp = __shfl_sync(kAll, szp[c], y);
+				const uint32_t zl = __shfl_up_sync(kAll, m, 1), zr = __shfl_down_sync(kAll, m, 1);
+				uint32_t d = (m << 1) | (m >> 1) | up[c] | dn;
+				d |= (xm >> lane) & 1u;
+				d |= ((xp >> lane) & 1u) << 31;
+				d |= lane > 0 ? zl : zm;
+				d |= lane < 31 ? zr : zp;
+				uint32_t s = m | (pass[j] & d);
+				if (c == 1) { // emitters below level 15: each row of the layer that holds some, by the whole warp
+					for (uint32_t rows = lowy; rows; rows &= rows - 1) {
+						const int z = __ffs(rows) - 1;
+						const uint16_t b = __ldg(L.blocks + (size_t)slot * 32768 + (y * 32 + z) * 32 + lane);
+						const uint32_t seeded = __ballot_sync(kAll, T.classes[T.class_of[b]].light >= t);
+						if (lane == z)
+							s |= seeded;
+					}
+				}
+				any[c] |= s != 0, all[c] &= s == kAll;
+				lev[(size_t)(c * kLevels + t - 1) * kPlaneWords + y * 32 + lane] = s;
+				const uint32_t lo = __ballot_sync(kAll, s & 1u), hi = __ballot_sync(kAll, s >> 31);
+				if (lane == y)
+					elo[c] = lo, ehi[c] = hi;
+				up[c] = m;
+				me[c] = dn;
 			}
 		}
 	}
@@ -651,14 +653,14 @@ __global__ void __launch_bounds__(kLightThreads, 16) k_light_level(LightPass L, 
 	for (int c = 0; c < 2; ++c) {
 		if (!((run >> c) & 1u))
 			continue;
-		const bool a = __syncthreads_or(any[c]), f = __syncthreads_and(all[c]);
-		if (tid == 0 && (!a || f))
+		uint32_t *e = edg + (size_t)(c * kLevels + t - 1) * 64;
+		e[lane] = elo[c];
+		e[32 + lane] = ehi[c];
+		const bool a = __any_sync(kAll, any[c]), f = __all_sync(kAll, all[c]);
+		if (lane == 0 && (!a || f))
 			atomicOr(L.flags + 2 * (size_t)i + c, !a ? 1u << (t - 1) : 1u << (kFlagFull + t - 1));
-		if (a && t > 1 && tid < 7) {
-			const int nb = tid < 6 ? s_nb[tid] : i;
-			if (nb >= 0)
-				atomicOr(L.near + 2 * (size_t)nb + c, 1u << (t - 2));
-		}
+		if (a && t > 1 && lane < 7 && near_nb >= 0) // lanes 0-6: faces 0-5, then the chunk
+			atomicOr(L.near + 2 * (size_t)near_nb + c, 1u << (t - 2));
 	}
 }
 
@@ -738,6 +740,32 @@ __device__ __forceinline__ bool light_item(Smem &S, int it, uint64_t v[4]) {
 		light[2 * lt_index(x, y, z0)] = (uint8_t)q;
 	}
 	return false;
+}
+
+// Light bytes of the chunk's own row (y, z), both in [0, 32), from its 15 nested level planes per
+// channel: uniform planes as constants, the planes staged in shared memory (`staged`, slot
+// S.lvl_slot[plane] of 1,024 words each) from there, the others from global memory.
+__device__ __forceinline__ void light_own_row(const Smem &S, int y, int z, const uint32_t *staged, uint64_t v[4]) {
+	const int w = y * 32 + z;
+	uint32_t b[2][4];
+#pragma unroll
+	for (int c = 0; c < 2; ++c) {
+		const uint32_t fl = S.lfl[26][c];
+		uint32_t lv[kLevels];
+#pragma unroll
+		for (int u = 0; u < kLevels; ++u) {
+			const int slot = S.lvl_slot[c * kLevels + u];
+			lv[u] = level_empty(fl, u + 1) ? 0u
+			        : level_full(fl, u + 1) ? 0xffffffffu
+			        : slot >= 0 ? staged[slot * kPlaneWords + w]
+			                    : __ldg(S.lvl[26] + (size_t)(c * kLevels + u) * kPlaneWords + w);
+		}
+		level_bits(lv, b[c]);
+	}
+	const uint32_t q[8] = {b[0][0], b[0][1], b[0][2], b[0][3], b[1][0], b[1][1], b[1][2], b[1][3]};
+#pragma unroll
+	for (int g = 0; g < 4; ++g)
+		v[g] = light_bytes8(q, g);
 }
 
 // Writes the 32 cells x in [0, 32) of row item `row` (34 * (y + 1) + z + 1): light bytes from v,
