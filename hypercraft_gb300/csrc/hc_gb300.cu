@@ -1006,7 +1006,7 @@ hc_status enqueue_plan(hc_batch_plan *p, cudaStream_t st) {
 		                  p->d_edges, p->d_lflags, p->d_lflags + 2 * (size_t)p->n_slots, p->n_slots};
 		HC_CUDA(ctx, cudaMemsetAsync(L.near, 0, 2 * (size_t)p->n_slots * sizeof(uint32_t), st));
 		for (int t = kLevels; t >= 1; --t) {
-			k_light_level<<<(p->n_slots + kLightWarps - 1) / kLightWarps, kLightThreads, 0, st>>>(L, tables(ctx), t);
+			k_light_level<<<(2 * p->n_slots + kLightWarps - 1) / kLightWarps, kLightThreads, 0, st>>>(L, tables(ctx), t);
 			HC_CUDA(ctx, cudaGetLastError());
 		}
 	}

@@ -395,8 +395,9 @@ __device__ __forceinline__ void planes_row(const uint16_t *blk, const int8_t *hg
 constexpr int kLevels = 15;
 constexpr size_t kLevelSlotWords = (size_t)2 * kLevels * kPlaneWords; // per chunk: 2 channels x 15 levels
 constexpr size_t kEdgeSlotWords = (size_t)2 * kLevels * 2 * 32;       // per chunk: x = 0 and x = 31 bits
-constexpr int kLightWarps = 4;                                         // chunks per block, one warp each
+constexpr int kLightWarps = 4;       // warps per block, one chunk channel each
 constexpr int kLightThreads = 32 * kLightWarps;
+constexpr int kLightBlocksPerSM = 12; // register bound: 40 per thread
 
 struct LightPass {
 	const int32_t *slots;   // batch chunk -> pool slot
@@ -442,226 +443,159 @@ __device__ __forceinline__ void level_bits(const uint32_t *s, uint32_t b[4]) {
 	           mux(b[2], mux(b[1], s[6], s[4]), mux(b[1], s[2], s[0])));
 }
 
-// Level t of every batch chunk, one warp per chunk (lane = z): the warp walks the chunk's 32 y
-// layers, keeping the level t + 1 rows of layers y - 1, y and y + 1 in registers, and dilates both
-// channels of each layer with shifts (x), shuffles (z) and the neighbouring layers (y). The face
+// Level t of every batch chunk, one warp per chunk and channel (lane = z): the warp walks the
+// chunk's 32 y layers, keeping the level t + 1 rows of layers y - 1, y and y + 1 in registers, and
+// dilates each layer with shifts (x), shuffles (z) and the neighbouring layers (y). The face
 // neighbours' touching rows and edge bits are loaded once, one word per lane. Also writes the row
 // edge bits that the x neighbours read at the next level, and the plane's uniform bits
 // (LightPass::flags). A channel whose level follows from level t + 1 without computing (see kFlag*)
-// is skipped: a chunk of sunlit air far from any emitter costs one flag word per level. No block
-// barrier: the warps of a block are independent chunks.
-__global__ void __launch_bounds__(kLightThreads, 8) k_light_level(LightPass L, DevTables T, int t) {
+// is skipped: a chunk of sunlit air far from any emitter costs one flag word per level and channel.
+// No block barrier: the warps of a block are independent.
+__global__ void __launch_bounds__(kLightThreads, kLightBlocksPerSM) k_light_level(LightPass L, DevTables T, int t) {
 	constexpr uint32_t kAll = 0xffffffffu;
 	const int lane = threadIdx.x & 31;
-	const uint32_t i = blockIdx.x * kLightWarps + (threadIdx.x >> 5);
+	const uint32_t w = blockIdx.x * kLightWarps + (threadIdx.x >> 5);
+	const uint32_t i = w >> 1;
+	const int c = (int)(w & 1u); // 0: sun, 1: torch
 	if (i >= L.n) // the whole warp
 		return;
-	// lanes 0-5: the face neighbours; lane 6: the pool slot; lanes 8-9: the flags; lanes 10-11: the
-	// near bits (flags and near bits from level t + 1)
+	// lanes 0-5: the face neighbours; lane 6: the pool slot; lane 8: the channel's flags; lane 10:
+	// its near bits (flags and near bits from level t + 1)
 	int32_t v1 = -1;
 	if (lane < 6)
 		v1 = __ldg(L.nb6 + 6 * (size_t)i + lane);
 	else if (lane == 6)
 		v1 = __ldg(L.slots + i);
-	else if (t < kLevels && lane >= 8 && lane < 10)
-		v1 = (int32_t)__ldg(L.flags + 2 * (size_t)i + (lane - 8));
-	else if (t < kLevels && lane >= 10 && lane < 12)
-		v1 = (int32_t)__ldg(L.near + 2 * (size_t)i + (lane - 10));
+	else if (t < kLevels && lane == 8)
+		v1 = (int32_t)__ldg(L.flags + 2 * (size_t)i + c);
+	else if (t < kLevels && lane == 10)
+		v1 = (int32_t)__ldg(L.near + 2 * (size_t)i + c);
 	const int slot = __shfl_sync(kAll, v1, 6);
-	// lane l < 14: channel l / 7 and face l % 7 (6 = the chunk itself), for the near bits it sets
-	const int nb7 = __shfl_sync(kAll, v1, lane % 7 < 6 ? lane % 7 : 0);
-	const int near_nb = lane % 7 < 6 ? nb7 : (int)i;
+	const int near_nb = lane < 6 ? v1 : (int)i; // lanes 0-6: the chunks whose near bits this one sets
 	const uint32_t *P = L.planes + (size_t)slot * kPlaneStride;
-	uint32_t *const lev = L.levels + (size_t)i * kLevelSlotWords;
-	uint32_t *const edg = L.edges + (size_t)i * kEdgeSlotWords;
+	uint32_t *const lev = L.levels + (size_t)i * kLevelSlotWords + (size_t)c * kLevels * kPlaneWords;
+	uint32_t *const edg = L.edges + (size_t)i * kEdgeSlotWords + (size_t)c * kLevels * 64;
+	uint32_t *const flag = L.flags + 2 * (size_t)i + c;
 	if (t == kLevels) { // the seeds: sunlit cells, emitters of level 15 (uniform planes are not stored)
-		const uint32_t low = __ldg(P + kPlaneLowOff + lane);
-		bool any[2] = {false, false}, all[2] = {true, true};
+		const uint32_t *seed = P + (c ? kPlaneT15 : kPlaneSun) * kPlaneWords;
+		bool any = false, all = true;
 #pragma unroll 8
 		for (int y = 0; y < 32; ++y) {
-			const uint32_t s0 = __ldg(P + kPlaneSun * kPlaneWords + y * 32 + lane);
-			const uint32_t s1 = __ldg(P + kPlaneT15 * kPlaneWords + y * 32 + lane);
-			any[0] |= s0 != 0, all[0] &= s0 == kAll;
-			any[1] |= s1 != 0, all[1] &= s1 == kAll;
+			const uint32_t s = __ldg(seed + y * 32 + lane);
+			any |= s != 0, all &= s == kAll;
 		}
-		uint32_t fl[2];
-		bool store[2];
-#pragma unroll
-		for (int c = 0; c < 2; ++c) {
-			const bool a = __any_sync(kAll, any[c]), f = __all_sync(kAll, all[c]);
-			fl[c] = (a ? 0u : 1u << (kLevels - 1)) | (f ? 1u << (kFlagFull + kLevels - 1) : 0u);
-			store[c] = a && !f;
-		}
-		fl[1] |= __any_sync(kAll, low != 0) ? kFlagLowEmitters : 0u;
-		if (store[0] || store[1]) { // the rows again (in L1 now), stored with their edge bits
-			uint32_t elo[2] = {0u, 0u}, ehi[2] = {0u, 0u};
+		const bool a = __any_sync(kAll, any), f = __all_sync(kAll, all);
+		uint32_t fl = (a ? 0u : 1u << (kLevels - 1)) | (f ? 1u << (kFlagFull + kLevels - 1) : 0u);
+		if (c == 1)
+			fl |= __any_sync(kAll, __ldg(P + kPlaneLowOff + lane) != 0) ? kFlagLowEmitters : 0u;
+		if (a && !f) { // the rows again (in L1 now), stored with their edge bits
+			uint32_t elo = 0u, ehi = 0u;
+			uint32_t *out = lev + (size_t)(kLevels - 1) * kPlaneWords;
 #pragma unroll 8
 			for (int y = 0; y < 32; ++y) {
-#pragma unroll
-				for (int c = 0; c < 2; ++c) {
-					if (!store[c])
-						continue;
-					const uint32_t s = __ldg(P + (c ? kPlaneT15 : kPlaneSun) * kPlaneWords + y * 32 + lane);
-					lev[(size_t)(c * kLevels + kLevels - 1) * kPlaneWords + y * 32 + lane] = s;
-					const uint32_t lo = __ballot_sync(kAll, s & 1u), hi = __ballot_sync(kAll, s >> 31);
-					if (lane == y)
-						elo[c] = lo, ehi[c] = hi;
-				}
+				const uint32_t s = __ldg(seed + y * 32 + lane);
+				out[y * 32 + lane] = s;
+				const uint32_t lo = __ballot_sync(kAll, s & 1u), hi = __ballot_sync(kAll, s >> 31);
+				if (lane == y)
+					elo = lo, ehi = hi;
 			}
-#pragma unroll
-			for (int c = 0; c < 2; ++c) {
-				if (!store[c])
-					continue;
-				uint32_t *e = edg + (size_t)(c * kLevels + kLevels - 1) * 64;
-				e[lane] = elo[c];
-				e[32 + lane] = ehi[c];
-			}
+			uint32_t *e = edg + (size_t)(kLevels - 1) * 64;
+			e[lane] = elo;
+			e[32 + lane] = ehi;
 		}
-		if (lane < 2)
-			L.flags[2 * (size_t)i + lane] = lane ? fl[1] : fl[0];
-		if (lane < 14) { // a non-empty level 15 may light this chunk and its face neighbours at level 14
-			const int c = lane / 7;
-			if (near_nb >= 0 && !level_empty(c ? fl[1] : fl[0], kLevels))
-				atomicOr(L.near + 2 * (size_t)near_nb + c, 1u << (kLevels - 2));
-		}
+		if (lane == 0)
+			*flag = fl;
+		if (a && lane < 7 && near_nb >= 0) // a non-empty level 15 may light the chunk and its face neighbours at level 14
+			atomicOr(L.near + 2 * (size_t)near_nb + c, 1u << (kLevels - 2));
 		return;
 	}
-	const uint32_t own[2] = {(uint32_t)__shfl_sync(kAll, v1, 8), (uint32_t)__shfl_sync(kAll, v1, 9)};
-	const uint32_t nr[2] = {(uint32_t)__shfl_sync(kAll, v1, 10), (uint32_t)__shfl_sync(kAll, v1, 11)};
-	// which channels follow from level t + 1 without computing: full stays full; empty stays empty
+	const uint32_t own = (uint32_t)__shfl_sync(kAll, v1, 8), nr = (uint32_t)__shfl_sync(kAll, v1, 10);
+	// a channel that follows from level t + 1 without computing: full stays full; empty stays empty
 	// when no face neighbour had light at level t + 1 and no emitter seeds level t
-	uint32_t run = 0;
-#pragma unroll
-	for (int c = 0; c < 2; ++c) {
-		const bool full = level_full(own[c], t + 1);
-		const bool trivial = full || (level_empty(own[c], t + 1) && !((nr[c] >> (t - 1)) & 1u) &&
-		                              !(c == 1 && (own[c] & kFlagLowEmitters)));
-		if (!trivial)
-			run |= 1u << c;
-		else if (lane == c)
-			atomicOr(L.flags + 2 * (size_t)i + c, full ? 1u << (kFlagFull + t - 1) : 1u << (t - 1));
-	}
-	// a full plane at level t (it stays full) lights this chunk and its face neighbours at level t - 1
-	if (t > 1 && lane < 14) {
-		const int c = lane / 7;
-		if (near_nb >= 0 && !((run >> c) & 1u) && level_full(c ? own[1] : own[0], t + 1))
+	const bool full = level_full(own, t + 1);
+	if (full || (level_empty(own, t + 1) && !((nr >> (t - 1)) & 1u) && !(c == 1 && (own & kFlagLowEmitters)))) {
+		if (lane == 0)
+			atomicOr(flag, full ? 1u << (kFlagFull + t - 1) : 1u << (t - 1));
+		// a full plane at level t (it stays full) lights the chunk and its face neighbours at level t - 1
+		if (full && t > 1 && lane < 7 && near_nb >= 0)
 			atomicOr(L.near + 2 * (size_t)near_nb + c, 1u << (t - 2));
-	}
-	if (!run)
 		return;
-	// lanes 0-11: the neighbours' level t + 1 flags, face lane / 2, channel lane % 2 (a missing
-	// neighbour is dark: empty)
-	const int nbq = __shfl_sync(kAll, v1, lane < 12 ? lane >> 1 : 0);
-	uint32_t nfl = 0xffffu;
-	if (lane < 12 && nbq >= 0)
-		nfl = __ldg(L.flags + 2 * (size_t)nbq + (lane & 1));
-	int nb[6];
+	}
+	// lanes 0-5: the face neighbours' level t + 1 flags (a missing neighbour is dark: empty)
+	const uint32_t nfl = lane < 6 && v1 >= 0 ? __ldg(L.flags + 2 * (size_t)v1 + c) : 0xffffu;
+	// lane k: x = -1 bits over z of layer k, x = 32 bits, the y = -1 and y = 32 rows at z = k, the
+	// z = -1 and z = 32 rows of layer k
+	uint32_t side[6];
 #pragma unroll
-	for (int f = 0; f < 6; ++f)
-		nb[f] = __shfl_sync(kAll, v1, f);
-	// per channel, lane k: x = -1 bits over z of layer k, x = 32 bits, the y = -1 and y = 32 rows
-	// at z = k, the z = -1 and z = 32 rows of layer k
-	uint32_t sxm[2], sxp[2], sym[2], syp[2], szm[2], szp[2];
-#pragma unroll
-	for (int c = 0; c < 2; ++c) {
-		uint32_t fl[6];
-#pragma unroll
-		for (int f = 0; f < 6; ++f)
-			fl[f] = __shfl_sync(kAll, nfl, 2 * f + c);
-		sxm[c] = sxp[c] = sym[c] = syp[c] = szm[c] = szp[c] = 0u;
-		if (!((run >> c) & 1u))
+	for (int f = 0; f < 6; ++f) {
+		const int nb = __shfl_sync(kAll, v1, f);
+		const uint32_t fl = __shfl_sync(kAll, nfl, f);
+		side[f] = 0u;
+		if (nb < 0)
 			continue;
-		if (nb[0] >= 0)
-			sxm[c] = level_word(fl[0], t + 1, level_edges(L, nb[0], c, t + 1) + 32 + lane);
-		if (nb[1] >= 0)
-			sxp[c] = level_word(fl[1], t + 1, level_edges(L, nb[1], c, t + 1) + lane);
-		if (nb[2] >= 0)
-			sym[c] = level_word(fl[2], t + 1, level_plane(L, nb[2], c, t + 1) + 31 * 32 + lane);
-		if (nb[3] >= 0)
-			syp[c] = level_word(fl[3], t + 1, level_plane(L, nb[3], c, t + 1) + lane);
-		if (nb[4] >= 0)
-			szm[c] = level_word(fl[4], t + 1, level_plane(L, nb[4], c, t + 1) + lane * 32 + 31);
-		if (nb[5] >= 0)
-			szp[c] = level_word(fl[5], t + 1, level_plane(L, nb[5], c, t + 1) + lane * 32);
+		const uint32_t *e = L.edges + (size_t)nb * kEdgeSlotWords + (size_t)(c * kLevels + t) * 64;
+		const uint32_t *p = L.levels + (size_t)nb * kLevelSlotWords + (size_t)(c * kLevels + t) * kPlaneWords;
+		const int off = f == 0 ? 32 + lane : f == 1 ? lane : f == 2 ? 31 * 32 + lane : f == 3 ? lane
+		              : f == 4 ? lane * 32 + 31 : lane * 32;
+		side[f] = level_word(fl, t + 1, (f < 2 ? e : p) + off);
 	}
 	// the chunk's own level t + 1 rows: stored, or a constant (a computed channel's level t + 1 is
 	// stored or empty)
-	const uint32_t *src[2] = {level_plane(L, i, 0, t + 1), level_plane(L, i, 1, t + 1)};
-	const bool stored[2] = {!level_empty(own[0], t + 1) && !level_full(own[0], t + 1),
-	                        !level_empty(own[1], t + 1) && !level_full(own[1], t + 1)};
-	const uint32_t cst[2] = {level_full(own[0], t + 1) ? kAll : 0u, level_full(own[1], t + 1) ? kAll : 0u};
-	const uint32_t lows = (run & 2u) ? __ldg(P + kPlaneLowOff + lane) : 0u; // lane y: low-emitter rows of layer y
-	uint32_t up[2], me[2];
-#pragma unroll
-	for (int c = 0; c < 2; ++c) {
-		up[c] = sym[c];
-		me[c] = stored[c] ? __ldg(src[c] + lane) : cst[c];
-	}
-	uint32_t elo[2] = {0u, 0u}, ehi[2] = {0u, 0u};
-	bool any[2] = {false, false}, all[2] = {true, true};
+	const uint32_t *src = lev + (size_t)t * kPlaneWords;
+	const bool stored = !level_empty(own, t + 1);
+	const uint32_t lows = c == 1 ? __ldg(P + kPlaneLowOff + lane) : 0u; // lane y: low-emitter rows of layer y
+	uint32_t up = side[2], me = stored ? __ldg(src + lane) : 0u;
+	uint32_t elo = 0u, ehi = 0u, any = 0u, all = kAll;
+	uint32_t *out = lev + (size_t)(t - 1) * kPlaneWords;
 	constexpr int kBatch = 8; // layers whose rows are requested together
 	for (int y0 = 0; y0 < 32; y0 += kBatch) {
-		uint32_t pass[kBatch], next[2][kBatch];
+		uint32_t pass[kBatch], next[kBatch];
 #pragma unroll
 		for (int j = 0; j < kBatch; ++j) {
 			const int y = y0 + j;
 			pass[j] = __ldg(P + kPlanePass * kPlaneWords + y * 32 + lane);
-#pragma unroll
-			for (int c = 0; c < 2; ++c)
-				next[c][j] = y < 31 ? (stored[c] ? __ldg(src[c] + (y + 1) * 32 + lane) : cst[c]) : syp[c];
+			next[j] = y < 31 ? (stored ? __ldg(src + (y + 1) * 32 + lane) : 0u) : side[3];
 		}
 #pragma unroll
 		for (int j = 0; j < kBatch; ++j) {
 			const int y = y0 + j;
-			const uint32_t lowy = __shfl_sync(kAll, lows, y);
-#pragma unroll
-			for (int c = 0; c < 2; ++c) {
-				if (!((run >> c) & 1u))
-					continue;
-				const uint32_t m = me[c], dn = next[c][j];
-				const uint32_t xm = __shfl_sync(kAll, sxm[c], y), xp = __shfl_sync(kAll, sxp[c], y);
-				const uint32_t zm = __shfl_sync(kAll, szm[c], y), zp = __shfl_sync(kAll, szp[c], y);
-				const uint32_t zl = __shfl_up_sync(kAll, m, 1), zr = __shfl_down_sync(kAll, m, 1);
-				uint32_t d = (m << 1) | (m >> 1) | up[c] | dn;
-				d |= (xm >> lane) & 1u;
-				d |= ((xp >> lane) & 1u) << 31;
-				d |= lane > 0 ? zl : zm;
-				d |= lane < 31 ? zr : zp;
-				uint32_t s = m | (pass[j] & d);
-				if (c == 1) { // emitters below level 15: each row of the layer that holds some, by the whole warp
-					for (uint32_t rows = lowy; rows; rows &= rows - 1) {
-						const int z = __ffs(rows) - 1;
-						const uint16_t b = __ldg(L.blocks + (size_t)slot * 32768 + (y * 32 + z) * 32 + lane);
-						const uint32_t seeded = __ballot_sync(kAll, T.classes[T.class_of[b]].light >= t);
-						if (lane == z)
-							s |= seeded;
-					}
-				}
-				any[c] |= s != 0, all[c] &= s == kAll;
-				lev[(size_t)(c * kLevels + t - 1) * kPlaneWords + y * 32 + lane] = s;
-				const uint32_t lo = __ballot_sync(kAll, s & 1u), hi = __ballot_sync(kAll, s >> 31);
-				if (lane == y)
-					elo[c] = lo, ehi[c] = hi;
-				up[c] = m;
-				me[c] = dn;
+			const uint32_t m = me, dn = next[j];
+			const uint32_t xm = __shfl_sync(kAll, side[0], y), xp = __shfl_sync(kAll, side[1], y);
+			const uint32_t zm = __shfl_sync(kAll, side[4], y), zp = __shfl_sync(kAll, side[5], y);
+			const uint32_t zl = __shfl_up_sync(kAll, m, 1), zr = __shfl_down_sync(kAll, m, 1);
+			uint32_t d = (m << 1) | (m >> 1) | up | dn;
+			d |= (xm >> lane) & 1u;
+			d |= ((xp >> lane) & 1u) << 31;
+			d |= lane > 0 ? zl : zm;
+			d |= lane < 31 ? zr : zp;
+			uint32_t s = m | (pass[j] & d);
+			// emitters below level 15: each row of the layer that holds some, by the whole warp
+			for (uint32_t rows = __shfl_sync(kAll, lows, y); rows; rows &= rows - 1) {
+				const int z = __ffs(rows) - 1;
+				const uint16_t b = __ldg(L.blocks + (size_t)slot * 32768 + (y * 32 + z) * 32 + lane);
+				const uint32_t seeded = __ballot_sync(kAll, T.classes[T.class_of[b]].light >= t);
+				if (lane == z)
+					s |= seeded;
 			}
+			any |= s, all &= s;
+			out[y * 32 + lane] = s;
+			const uint32_t lo = __ballot_sync(kAll, s & 1u), hi = __ballot_sync(kAll, s >> 31);
+			if (lane == y)
+				elo = lo, ehi = hi;
+			up = m;
+			me = dn;
 		}
 	}
 	// a computed plane that came out uniform is flagged too (it is stored as well); a non-empty one
-	// lights this chunk and its face neighbours at level t - 1
-#pragma unroll
-	for (int c = 0; c < 2; ++c) {
-		if (!((run >> c) & 1u))
-			continue;
-		uint32_t *e = edg + (size_t)(c * kLevels + t - 1) * 64;
-		e[lane] = elo[c];
-		e[32 + lane] = ehi[c];
-		const bool a = __any_sync(kAll, any[c]), f = __all_sync(kAll, all[c]);
-		if (lane == 0 && (!a || f))
-			atomicOr(L.flags + 2 * (size_t)i + c, !a ? 1u << (t - 1) : 1u << (kFlagFull + t - 1));
-		if (a && t > 1 && lane < 7 && near_nb >= 0) // lanes 0-6: faces 0-5, then the chunk
-			atomicOr(L.near + 2 * (size_t)near_nb + c, 1u << (t - 2));
-	}
+	// lights the chunk and its face neighbours at level t - 1
+	uint32_t *e = edg + (size_t)(t - 1) * 64;
+	e[lane] = elo;
+	e[32 + lane] = ehi;
+	const bool a = __any_sync(kAll, any != 0), f = __all_sync(kAll, all == kAll);
+	if (lane == 0 && (!a || f))
+		atomicOr(flag, !a ? 1u << (t - 1) : 1u << (kFlagFull + t - 1));
+	if (a && t > 1 && lane < 7 && near_nb >= 0)
+		atomicOr(L.near + 2 * (size_t)near_nb + c, 1u << (t - 2));
 }
 
 // Light bytes of the eight cells x = 8g .. 8g + 7 from the eight digit planes of a row (sun digits
