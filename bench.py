@@ -91,9 +91,9 @@ def workload_name(workload, size=""):
 # of that launch (--metrics dram__bytes_read.sum,dram__bytes_write.sum, one pass) on the same
 # source; other workloads: null.
 MESH_TRAFFIC = {
-    "scale:32x8x32": {"bytes": 1.643e9, "capture": "k_mesh_batch, 3rd launch of "
+    "scale:32x8x32": {"bytes": 1.644e9, "capture": "k_mesh_batch, 3rd launch of "
                       "`bench.py --steps 2 --warmup 3 --no-plain --no-e2e --no-cpu --no-extra --variant 0`"},
-    "mixture:32x16x32": {"bytes": 13.570e9, "capture": "k_mesh_batch, 3rd launch of "
+    "mixture:32x16x32": {"bytes": 13.563e9, "capture": "k_mesh_batch, 3rd launch of "
                          "`bench.py --workload mixture --steps 2 --warmup 3 --no-plain --no-e2e --no-cpu --no-extra "
                          "--variant 0`"},
 }
@@ -101,9 +101,9 @@ MESH_TRAFFIC = {
 # What bounds the mesher instead of DRAM, from one ncu --set full capture per workload (a
 # 16 x 8 x 16 grid of the same world): issue-slot, ALU-pipe, DRAM and warp-occupancy fractions.
 MESH_LIMITER = {
-    "scale": {"issue_active_frac": 0.496, "alu_pipe_frac": 0.434, "dram_throughput_frac": 0.094,
-              "warps_active_frac": 0.500, "capture": "ncu --set full, k_mesh_batch, scale 16x8x16"},
-    "mixture": {"issue_active_frac": 0.618, "alu_pipe_frac": 0.590, "dram_throughput_frac": 0.122,
+    "scale": {"issue_active_frac": 0.499, "alu_pipe_frac": 0.435, "dram_throughput_frac": 0.098,
+              "warps_active_frac": 0.499, "capture": "ncu --set full, k_mesh_batch, scale 16x8x16"},
+    "mixture": {"issue_active_frac": 0.620, "alu_pipe_frac": 0.592, "dram_throughput_frac": 0.124,
                 "warps_active_frac": 0.500, "capture": "ncu --set full, k_mesh_batch, mixture 16x8x16"},
 }
 
