@@ -49,3 +49,19 @@ def test_context_without_gpu_fails_cleanly(built):
     h = ctypes.c_void_p()
     assert lib.hc_ctx_create(0, ctypes.byref(h)) == HC_ERR_NO_DEVICE
     assert not h.value
+
+
+def test_variant_tables_match_the_header():
+    """The Python mirror names every persistent variant the header enumerates, in its order, and
+    counts the light-pass variants' extra launches (15 light levels) in the launch claim."""
+    from hypercraft_gb300 import batch
+    text = open(os.path.join(REPO, "include", "hc_gb300.h")).read()
+    enum = dict((m.group(1), int(m.group(2))) for m in re.finditer(r"\bHC_VARIANT_(\w+)\s*=\s*(\d+)", text))
+    count = enum.pop("COUNT")
+    assert count == len(batch.VARIANTS) == len(enum)
+    assert sorted(enum.values()) == list(range(count))
+    light = {v for k, v in enum.items() if k in ("LIGHT_PASS", "CLAIM2", "CLAIM4", "NO_SCRATCH")}
+    assert light == set(batch.LIGHT_PASS_VARIANTS)
+    for v in range(count):
+        assert ("light pass" in batch.VARIANTS[v]) == (v in light)
+        assert batch.launches_per_run(v) == (18 if v in light else (3 if v == enum["WINDOW"] else 2))
